@@ -1,0 +1,328 @@
+"""Benchmark of the DG RHS / RK4 time-step path on GB300.
+
+Workload (default): the density-wave Euler case -- [0,1]^2 periodic, 2 x 1024^2
+= 2,097,152 triangles jittered by +-0.15h (seeded), Dubiner-order p = 3
+(n_p = 10), 4 conserved variables in FP32, LLF flux, classic RK4 with the
+reference's CFL rule (dt = 0.7 min diameter / max wave speed / (2p+1)) computed
+on the device each step.  One "step" is one full RK4 time step (CFL reduction
+plus four fused stage kernels); one DOF-update is one coefficient (element x
+mode x variable) advanced by one step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  ``--impl reference`` times the CPU restatement of the
+reference's per-edge / per-element loops (oracle/, FP64, all host threads) on
+a bounded sample of the same workload.  Under torchrun (N > 1) every rank runs
+an independent replica of the solve (the path has no data exchange between
+solves) and value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-updates/s on 1 GB300, served/batched vs plain at L2≤1e-5; p50/p99 latency"
+UNIT = "DOF-updates/s"
+WORKLOAD = dict(workload="euler_density_wave_2x1024^2_p3", equation="euler", order=3,
+                num_elem=2 * 1024 * 1024, mesh="periodic 2x1024^2, jitter 0.15h, seed 12347",
+                ic="rho=1+0.2 sin(2pi(x+y)), u=v=1, p=1, gamma=1.4", flux="LLF",
+                integrator="RK4, CFL 0.7 on device", precision="fp32",
+                l2_flush="inputs larger than L2 (4 state vectors x 335.5 MB)")
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (SM clock, reasons) taken while the bench runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0, period_ms: int = 100):
+        self.samples = []
+        self.proc = None
+        self.index = index
+        self.period = period_ms
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", f"-lms={self.period}"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), [x.strip() for x in line.split(",")]))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self, t0: float, t1: float):
+        win = [s for (t, s) in self.samples if t0 - 0.15 <= t <= t1 + 0.15]
+        if not win:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        sm = [float(s[1]) for s in win if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in win if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in win for i in range(4) if len(s) > 5 + i and s[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(win)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("DGX_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_mesh(n: int):
+    from dgcuda_gb300.mesh import periodic_square
+    return periodic_square(n, jitter=0.15, seed=12347)
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of the reference loops (FP64, OpenMP over all host cores)."""
+    if rank != 0:
+        return None
+    from oracle import oracle as orc
+    orc.build()
+    cores = orc.set_threads(os.cpu_count() or 1)
+    # size the per-step sample so that warm-up + timed steps take about two minutes
+    probe = build_mesh(64)
+    po = orc.Oracle(probe, 3, orc.EULER, orc.LLF, 1.4)
+    pc = po.project(orc.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
+    po.step(pc, po.cfl_dt(pc))
+    t0 = time.perf_counter()
+    po.step(pc, po.cfl_dt(pc))
+    per_elem = (time.perf_counter() - t0) / probe.num_elem
+    n_sample = 32
+    for n in (512, 256, 128, 64, 32):
+        if per_elem * 2 * n * n * (args.steps + args.warmup) <= 120.0:
+            n_sample = n
+            break
+    mesh = build_mesh(n_sample)
+    o = orc.Oracle(mesh, 3, orc.EULER, orc.LLF, 1.4)
+    c = o.project(orc.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
+    dofs = 4 * 10 * mesh.num_elem
+    for _ in range(args.warmup):
+        c = o.step(c, o.cfl_dt(c))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        c = o.step(c, o.cfl_dt(c))
+    el = time.perf_counter() - t0
+    value = dofs * args.steps / el
+    sample = (f"{args.steps} RK4 steps of the same scheme (p=3 Euler, LLF, CFL) on a 2x{n_sample}^2 "
+              f"periodic sub-problem ({mesh.num_elem} elements) of the 2x1024^2 workload, FP64")
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": WORKLOAD, "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def cpu_baseline_sample(budget_s: float = 12.0):
+    from oracle import oracle as orc
+    orc.build()
+    cores = orc.set_threads(os.cpu_count() or 1)
+    mesh = build_mesh(512)               # 2 x 512^2 = 524,288 elements
+    o = orc.Oracle(mesh, 3, orc.EULER, orc.LLF, 1.4)
+    c = o.project(orc.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
+    dofs = 4 * 10 * mesh.num_elem
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        c = o.step(c, o.cfl_dt(c))
+        steps += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or steps >= 20:
+            break
+    return {"value": dofs * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{steps} RK4 steps of the oracle (FP64 C restatement, OpenMP) on a 2x512^2 "
+                      f"periodic sub-problem ({mesh.num_elem} elements, p=3 Euler)"}
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    torch.cuda.set_device(local)
+    from dgcuda_gb300 import _ffi, build
+    from dgcuda_gb300.solver import Solver
+    build.build()
+    n = args.mesh_n
+    mesh = build_mesh(n)
+    E = mesh.num_elem
+    sv = Solver(mesh, 3, _ffi.EULER, _ffi.FLUX_LLF, _ffi.FP32, 1.4)
+    sv.project(_ffi.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
+    sv.set_dt(None, cfl=0.7)
+    sv.set_end_time(0.0)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    dofs = 4 * 10 * E
+    X = dofs * 4
+    G = 20 * E + 24 * mesh.num_sides
+    step_bytes = 16 * X + 4 * G                   # algorithmic bytes per RK4 step
+    # stages 2, 3, 4 move 5X + G, 5X + G and 3X + G (stage 1: 3X + G, timed with the CFL kernel)
+    stage_bytes = (13 * X + 3 * G) / 3.0          # per timed stage launch (average)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            sv.step(sh)
+        torch.cuda.synchronize()
+        launches0 = sv.launch_count()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+               torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        barrier(world)
+        torch.cuda.synchronize()
+        t_wall0 = time.time()
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            sv.rk_stage(0, sh)        # CFL reduction + dt, then stage 1
+            ev[i][1].record(stream)
+            sv.rk_stage(1, sh)
+            sv.rk_stage(2, sh)
+            sv.rk_stage(3, sh)
+            ev[i][2].record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        t_wall1 = time.time()
+        launches = sv.launch_count() - launches0
+    total_ms = ev[0][0].elapsed_time(ev[-1][2])
+    ms_step = allreduce_max(total_ms / args.steps, world)
+    stage_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / (3 * args.steps)   # stages 2-4
+    value = dofs * world / (ms_step * 1e-3)
+
+    # end to end through the C ABI with host buffers: pinned state in, step, state out
+    host = torch.empty(dofs, dtype=torch.float32, pin_memory=True)
+    sv.get_state_f32(host.numpy(), sh)
+    torch.cuda.synchronize()
+    e2e_steps = max(3, min(args.steps, 20))
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            sv.set_state_f32(host.numpy(), sh)
+            sv.step(sh)
+            sv.get_state_f32(host.numpy(), sh)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(e2e_steps):
+            sv.set_state_f32(host.numpy(), sh)
+            sv.step(sh)
+            sv.get_state_f32(host.numpy(), sh)
+        b.record(stream)
+        torch.cuda.synchronize()
+    e2e_ms = allreduce_max(a.elapsed_time(b) / e2e_steps, world)
+    clocks.stop()
+    ck = clocks.summary(t_wall0, t_wall1)
+    if rank != 0:
+        return None
+
+    peak, peak_src = peaks()
+    achieved = stage_bytes / (stage_ms * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "stage_kernel_density_wave_p3.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(WORKLOAD, num_elem=E, num_sides=mesh.num_sides, dofs=dofs,
+                       parallelism="replicas" if world > 1 else "single"),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "stage_kernel<3,EULER> (fused RK4 stage, FP32)",
+                     "algorithmic_bytes_per_launch": stage_bytes,
+                     "peak_source": f"{peak_src} hbm_gbs"},
+        "e2e": {"value": dofs * world / (e2e_ms * 1e-3), "unit": UNIT,
+                "h2d_bytes_per_step": X, "d2h_bytes_per_step": X,
+                "path": "dgx_set_state_f32 (pinned host) + dgx_step + dgx_get_state_f32"},
+        "clocks": ck,
+        "gpu_launches": launches,
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_sample()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--mesh-n", type=int, default=1024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_init()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_ours(args, rank, world, local)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,550 @@
+// dgx_api.cu -- the C ABI (include/dgx.h): meshes, solvers, state, RHS and
+// RK-stage calls.  Host orchestration only; the arithmetic is in
+// dgx_stage_f32.cu / dgx_stage_f64.cu / dgx_misc.cu.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "dgx_internal.h"
+
+namespace dgx {
+
+namespace {
+thread_local char g_err[512] = "";
+std::mutex g_init_mu;
+bool g_tables_ready[64] = {false};
+
+int ensure_device_tables() {
+    int dev = 0;
+    DGX_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) { set_error("device index %d out of range", dev); return DGX_ERR_UNSUPPORTED; }
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    if (g_tables_ready[dev]) return DGX_OK;
+    int rc = upload_tables_f32();
+    if (!rc) rc = upload_tables_f64();
+    if (!rc) rc = upload_tables_misc();
+    if (!rc) g_tables_ready[dev] = true;
+    return rc;
+}
+
+template <typename T>
+int dalloc(T **p, size_t count, size_t *acct) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+        return DGX_ERR_NOMEM;
+    }
+    if (acct) *acct += count * sizeof(T);
+    return DGX_OK;
+}
+
+void mesh_free(dgx_mesh *m) {
+    MeshDev &d = m->d;
+    void *ptrs[] = {d.V, d.elem_s, d.sides, d.J, d.xr, d.yr, d.xs, d.ys, d.diam, d.len, d.nx,
+                    d.ny, d.nbr, d.geo32, d.fn32, d.geo64, d.fn64};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete m;
+}
+
+void mesh_release(dgx_mesh *m) {
+    if (m && m->refs.fetch_sub(1) == 1) mesh_free(m);
+}
+
+cudaStream_t as_stream(void *s) { return static_cast<cudaStream_t>(s); }
+
+size_t elem_size(const SolverDev &s) { return s.precision == DGX_FP64 ? sizeof(double) : sizeof(float); }
+
+int stage_launch(dgx_solver *sv, int mode, const void *u, const void *c, void *acc, void *out,
+                 double dt, double t, cudaStream_t st) {
+    SolverDev &s = sv->s;
+    const MeshDev &m = sv->mesh->d;
+    StageArgs a;
+    a.E = m.num_elem;
+    a.mode = mode;
+    a.flux = s.flux;
+    a.gamma = s.gamma;
+    a.ax = s.ax;
+    a.ay = s.ay;
+    a.u = u;
+    a.c = c;
+    a.acc = acc;
+    a.out = out;
+    a.nbr = m.nbr;
+    a.scal = s.scal;
+    a.dt = dt;
+    a.t = t;
+    int rc;
+    if (s.precision == DGX_FP64) {
+        a.geo = m.geo64;
+        a.fn = m.fn64;
+        rc = launch_stage_f64(s.order, s.equation, a, st);
+    } else {
+        a.geo = m.geo32;
+        a.fn = m.fn32;
+        rc = launch_stage_f32(s.order, s.equation, a, st);
+    }
+    if (!rc) sv->launches++;
+    return rc;
+}
+
+int run_stage(dgx_solver *sv, int stage, cudaStream_t st) {
+    SolverDev &s = sv->s;
+    int rc;
+    switch (stage) {
+    case 0:
+        rc = launch_dt(s, sv->mesh->d, st);
+        if (rc) return rc;
+        sv->launches++;
+        return stage_launch(sv, 1, s.c, s.c, s.acc, s.ua, 0.0, 0.0, st);
+    case 1: return stage_launch(sv, 2, s.ua, s.c, s.acc, s.ub, 0.0, 0.0, st);
+    case 2: return stage_launch(sv, 3, s.ub, s.c, s.acc, s.ua, 0.0, 0.0, st);
+    case 3: return stage_launch(sv, 4, s.ua, s.c, s.acc, s.c, 0.0, 0.0, st);
+    default: set_error("stage must be 0..3"); return DGX_ERR_INVALID;
+    }
+}
+
+int write_scalar(SolverDev &s, int idx, double v) {
+    DGX_TRY_CUDA(cudaMemcpy(s.scal + idx, &v, sizeof(double), cudaMemcpyHostToDevice));
+    return DGX_OK;
+}
+
+}  // namespace
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+}  // namespace dgx
+
+using namespace dgx;
+
+extern "C" {
+
+int dgx_version(void) { return DGX_VERSION; }
+
+const char *dgx_last_error(void) { return g_err; }
+
+const char *dgx_status_string(int status) {
+    switch (status) {
+    case DGX_OK: return "ok";
+    case DGX_ERR_INVALID: return "invalid argument";
+    case DGX_ERR_CUDA: return "CUDA error";
+    case DGX_ERR_NOMEM: return "out of memory";
+    case DGX_ERR_UNSUPPORTED: return "unsupported";
+    case DGX_ERR_NONFINITE: return "non-finite or unphysical state";
+    case DGX_ERR_BUSY: return "busy";
+    case DGX_ERR_NOT_FOUND: return "not found";
+    case DGX_ERR_TIMEOUT: return "timeout";
+    default: return "unknown status";
+    }
+}
+
+int dgx_tables(int p, int *dims, double *r1, double *r2, double *w, double *r_oned, double *w_oned,
+               double *basis, double *grad_x, double *grad_y, double *basis_side,
+               double *basis_vertex) {
+    if (p < 0 || p > kMaxOrder) { set_error("order %d outside 0..%d", p, kMaxOrder); return DGX_ERR_UNSUPPORTED; }
+    const Tables &T = tables(p);
+    if (dims) { dims[0] = T.np; dims[1] = T.nq; dims[2] = T.nq1; }
+    auto cp = [](double *dst, const double *src, int n) { if (dst) std::memcpy(dst, src, sizeof(double) * n); };
+    cp(r1, T.r1, T.nq);
+    cp(r2, T.r2, T.nq);
+    cp(w, T.w, T.nq);
+    cp(r_oned, T.s1, T.nq1);
+    cp(w_oned, T.w1, T.nq1);
+    cp(basis, T.phi, T.np * T.nq);
+    cp(grad_x, T.gx, T.np * T.nq);
+    cp(grad_y, T.gy, T.np * T.nq);
+    cp(basis_side, T.side, 3 * T.np * T.nq1);
+    cp(basis_vertex, T.vert, 3 * T.np);
+    return DGX_OK;
+}
+
+int dgx_mesh_create(int num_elem, int num_sides, const double *V1x, const double *V1y,
+                    const double *V2x, const double *V2y, const double *V3x, const double *V3y,
+                    const int *elem_s1, const int *elem_s2, const int *elem_s3,
+                    const int *left_elem, const int *right_elem, const int *left_side_number,
+                    const int *right_side_number, dgx_mesh **out) {
+    if (!out) { set_error("out is NULL"); return DGX_ERR_INVALID; }
+    *out = nullptr;
+    if (num_elem <= 0 || num_sides <= 0 || num_elem > (1 << 28)) {
+        set_error("num_elem must be in 1..2^28 and num_sides >= 1");
+        return DGX_ERR_INVALID;
+    }
+    const double *Vs[6] = {V1x, V1y, V2x, V2y, V3x, V3y};
+    const int *es[3] = {elem_s1, elem_s2, elem_s3};
+    const int *sd[4] = {left_elem, right_elem, left_side_number, right_side_number};
+    for (auto p : Vs) if (!p) { set_error("vertex array is NULL"); return DGX_ERR_INVALID; }
+    for (auto p : es) if (!p) { set_error("elem_s array is NULL"); return DGX_ERR_INVALID; }
+    for (auto p : sd) if (!p) { set_error("side array is NULL"); return DGX_ERR_INVALID; }
+    // host validation of the connectivity (the reference trusts its mesh file)
+    int nb = 0;
+    for (int s = 0; s < num_sides; ++s) {
+        const int L = left_elem[s], Rr = right_elem[s], ls = left_side_number[s], rs = right_side_number[s];
+        if (L < 0 || L >= num_elem || ls < 0 || ls > 2) { set_error("side %d: bad left element/side", s); return DGX_ERR_INVALID; }
+        if (es[ls][L] != s) { set_error("side %d: elem_s of its left element does not point back", s); return DGX_ERR_INVALID; }
+        if (Rr >= 0) {
+            if (Rr >= num_elem || rs < 0 || rs > 2) { set_error("side %d: bad right element/side", s); return DGX_ERR_INVALID; }
+            if (Rr == L) { set_error("side %d: left and right element coincide", s); return DGX_ERR_INVALID; }
+            if (es[rs][Rr] != s) { set_error("side %d: elem_s of its right element does not point back", s); return DGX_ERR_INVALID; }
+        } else {
+            if (Rr < -3) { set_error("side %d: boundary tag %d outside -3..-1", s, Rr); return DGX_ERR_INVALID; }
+            ++nb;
+        }
+    }
+    for (int e = 0; e < num_elem; ++e) {
+        for (int k = 0; k < 3; ++k)
+            if (es[k][e] < 0 || es[k][e] >= num_sides) { set_error("element %d: side index out of range", e); return DGX_ERR_INVALID; }
+        const double J = (V2x[e] - V1x[e]) * (V3y[e] - V1y[e]) - (V3x[e] - V1x[e]) * (V2y[e] - V1y[e]);
+        if (!(J > 0.0)) { set_error("element %d is not counter-clockwise (J = %g)", e, J); return DGX_ERR_INVALID; }
+    }
+
+    dgx_mesh *m = new (std::nothrow) dgx_mesh();
+    if (!m) { set_error("host allocation failed"); return DGX_ERR_NOMEM; }
+    cudaGetDevice(&m->device);
+    MeshDev &d = m->d;
+    d.num_elem = num_elem;
+    d.num_sides = num_sides;
+    d.num_boundary = nb;
+    const size_t E = num_elem, S = num_sides;
+    int rc = DGX_OK;
+    size_t acct = 0;
+    rc |= dalloc(&d.V, 6 * E, &acct);
+    rc |= dalloc(&d.elem_s, 3 * E, &acct);
+    rc |= dalloc(&d.sides, 4 * S, &acct);
+    rc |= dalloc(&d.J, E, &acct); rc |= dalloc(&d.xr, E, &acct); rc |= dalloc(&d.yr, E, &acct);
+    rc |= dalloc(&d.xs, E, &acct); rc |= dalloc(&d.ys, E, &acct); rc |= dalloc(&d.diam, E, &acct);
+    rc |= dalloc(&d.len, S, &acct); rc |= dalloc(&d.nx, S, &acct); rc |= dalloc(&d.ny, S, &acct);
+    rc |= dalloc(&d.nbr, 3 * E, &acct);
+    rc |= dalloc(&d.geo32, 5 * E, &acct); rc |= dalloc(&d.fn32, 9 * E, &acct);
+    rc |= dalloc(&d.geo64, 5 * E, &acct); rc |= dalloc(&d.fn64, 9 * E, &acct);
+    if (rc) { mesh_free(m); return DGX_ERR_NOMEM; }
+    cudaError_t ce = cudaSuccess;
+    for (int i = 0; i < 6 && ce == cudaSuccess; ++i)
+        ce = cudaMemcpy(d.V + i * E, Vs[i], E * sizeof(double), cudaMemcpyHostToDevice);
+    for (int i = 0; i < 3 && ce == cudaSuccess; ++i)
+        ce = cudaMemcpy(d.elem_s + i * E, es[i], E * sizeof(int), cudaMemcpyHostToDevice);
+    for (int i = 0; i < 4 && ce == cudaSuccess; ++i)
+        ce = cudaMemcpy(d.sides + i * S, sd[i], S * sizeof(int), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) { set_error("mesh upload failed: %s", cudaGetErrorString(ce)); mesh_free(m); return DGX_ERR_CUDA; }
+    rc = mesh_geometry(d, nullptr);
+    if (!rc && cudaDeviceSynchronize() != cudaSuccess) { set_error("geometry kernels failed"); rc = DGX_ERR_CUDA; }
+    if (rc) { mesh_free(m); return rc; }
+    *out = m;
+    return DGX_OK;
+}
+
+int dgx_mesh_destroy(dgx_mesh *mesh) {
+    if (!mesh) return DGX_ERR_INVALID;
+    mesh_release(mesh);
+    return DGX_OK;
+}
+
+int dgx_mesh_geometry(const dgx_mesh *mesh, double *J, double *xr, double *yr, double *xs,
+                      double *ys, double *diameter, double *s_length, double *Nx, double *Ny) {
+    if (!mesh) return DGX_ERR_INVALID;
+    const MeshDev &d = mesh->d;
+    const size_t E = d.num_elem * sizeof(double), S = d.num_sides * sizeof(double);
+    struct { double *h; const double *dv; size_t n; } cps[] = {
+        {J, d.J, E}, {xr, d.xr, E}, {yr, d.yr, E}, {xs, d.xs, E}, {ys, d.ys, E},
+        {diameter, d.diam, E}, {s_length, d.len, S}, {Nx, d.nx, S}, {Ny, d.ny, S}};
+    for (auto &c : cps)
+        if (c.h) DGX_TRY_CUDA(cudaMemcpy(c.h, c.dv, c.n, cudaMemcpyDeviceToHost));
+    return DGX_OK;
+}
+
+int dgx_mesh_min_diameter(const dgx_mesh *mesh, double *out) {
+    if (!mesh || !out) return DGX_ERR_INVALID;
+    *out = mesh->d.min_diam;
+    return DGX_OK;
+}
+
+int dgx_mesh_info(const dgx_mesh *mesh, int *num_elem, int *num_sides, int *num_boundary) {
+    if (!mesh) return DGX_ERR_INVALID;
+    if (num_elem) *num_elem = mesh->d.num_elem;
+    if (num_sides) *num_sides = mesh->d.num_sides;
+    if (num_boundary) *num_boundary = mesh->d.num_boundary;
+    return DGX_OK;
+}
+
+int dgx_solver_create(dgx_mesh *mesh, const dgx_solver_desc *desc, dgx_solver **out) {
+    if (!mesh || !desc || !out) { set_error("NULL argument"); return DGX_ERR_INVALID; }
+    *out = nullptr;
+    if (desc->order < 0 || desc->order > kMaxOrder) { set_error("order %d outside 0..%d", desc->order, kMaxOrder); return DGX_ERR_UNSUPPORTED; }
+    if (desc->equation != DGX_ADVECTION && desc->equation != DGX_EULER) { set_error("unknown equation"); return DGX_ERR_INVALID; }
+    if (desc->flux != DGX_FLUX_CENTRAL && desc->flux != DGX_FLUX_LLF) { set_error("unknown flux"); return DGX_ERR_INVALID; }
+    if (desc->precision != DGX_FP32 && desc->precision != DGX_FP64) {
+        set_error("precision %d is not served by this build", desc->precision);
+        return DGX_ERR_UNSUPPORTED;
+    }
+    if (desc->integrator != DGX_RK4) { set_error("integrator %d is not served by this build", desc->integrator); return DGX_ERR_UNSUPPORTED; }
+    if (desc->equation == DGX_EULER && !(desc->gamma > 1.0)) { set_error("gamma must be > 1"); return DGX_ERR_INVALID; }
+    if (mesh->d.num_boundary > 0) {
+        set_error("meshes with boundary sides are not served by this build (periodic meshes only)");
+        return DGX_ERR_UNSUPPORTED;
+    }
+    int rc = ensure_device_tables();
+    if (rc) return rc;
+    dgx_solver *sv = new (std::nothrow) dgx_solver();
+    if (!sv) { set_error("host allocation failed"); return DGX_ERR_NOMEM; }
+    SolverDev &s = sv->s;
+    s.order = desc->order;
+    s.np = num_modes(desc->order);
+    s.nv = desc->equation == DGX_EULER ? 4 : 1;
+    s.equation = desc->equation;
+    s.flux = desc->flux;
+    s.precision = desc->precision;
+    s.gamma = desc->gamma;
+    s.ax = desc->ax;
+    s.ay = desc->ay;
+    s.n = static_cast<size_t>(s.nv) * s.np * mesh->d.num_elem;
+    const size_t es = elem_size(s);
+    size_t acct = 0;
+    char *bufs[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int i = 0; i < 4 && !rc; ++i) rc = dalloc(&bufs[i], s.n * es, &acct);
+    if (!rc) rc = dalloc(&s.scal, 8, &acct);
+    if (!rc) rc = dalloc(&s.lam_bits, 1, &acct);
+    if (!rc) rc = dalloc(&s.counter, 1, &acct);
+    if (!rc) rc = dalloc(&s.status, 1, &acct);
+    if (!rc) rc = dalloc(&s.steps, 1, &acct);
+    s.c = bufs[0]; s.acc = bufs[1]; s.ua = bufs[2]; s.ub = bufs[3];
+    if (!rc) {
+        const double init[8] = {0.0, 0.0, 0.0, 0.0, 0.7, 0.0, 0.0, 0.0};
+        cudaError_t ce = cudaMemcpy(s.scal, init, sizeof(init), cudaMemcpyHostToDevice);
+        if (ce == cudaSuccess) ce = cudaMemset(s.lam_bits, 0, sizeof(unsigned long long));
+        if (ce == cudaSuccess) ce = cudaMemset(s.counter, 0, sizeof(unsigned int));
+        if (ce == cudaSuccess) ce = cudaMemset(s.status, 0, sizeof(unsigned int));
+        if (ce == cudaSuccess) ce = cudaMemset(s.steps, 0, sizeof(long long));
+        if (ce == cudaSuccess) ce = cudaMemset(s.c, 0, s.n * es);
+        if (ce != cudaSuccess) { set_error("solver init failed: %s", cudaGetErrorString(ce)); rc = DGX_ERR_CUDA; }
+    }
+    if (rc) {
+        sv->mesh = nullptr;
+        dgx_solver_destroy(sv);
+        return rc;
+    }
+    mesh->refs.fetch_add(1);
+    sv->mesh = mesh;
+    sv->device_bytes = acct;
+    *out = sv;
+    return DGX_OK;
+}
+
+int dgx_solver_destroy(dgx_solver *sv) {
+    if (!sv) return DGX_ERR_INVALID;
+    SolverDev &s = sv->s;
+    void *ptrs[] = {s.c, s.acc, s.ua, s.ub, s.scal, s.lam_bits, s.counter, s.status, s.steps};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (sv->mesh) mesh_release(sv->mesh);
+    delete sv;
+    return DGX_OK;
+}
+
+int dgx_solver_info(const dgx_solver *sv, int *num_vars, int *n_p, size_t *state_bytes,
+                    size_t *device_bytes) {
+    if (!sv) return DGX_ERR_INVALID;
+    if (num_vars) *num_vars = sv->s.nv;
+    if (n_p) *n_p = sv->s.np;
+    if (state_bytes) *state_bytes = sv->s.n * elem_size(sv->s);
+    if (device_bytes) *device_bytes = sv->device_bytes;
+    return DGX_OK;
+}
+
+int dgx_set_state(dgx_solver *sv, const double *c) {
+    if (!sv || !c) return DGX_ERR_INVALID;
+    SolverDev &s = sv->s;
+    if (s.precision == DGX_FP64) {
+        DGX_TRY_CUDA(cudaMemcpy(s.c, c, s.n * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> tmp(s.n);
+        for (size_t i = 0; i < s.n; ++i) tmp[i] = static_cast<float>(c[i]);
+        DGX_TRY_CUDA(cudaMemcpy(s.c, tmp.data(), s.n * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    return DGX_OK;
+}
+
+int dgx_get_state(dgx_solver *sv, double *c) {
+    if (!sv || !c) return DGX_ERR_INVALID;
+    SolverDev &s = sv->s;
+    DGX_TRY_CUDA(cudaDeviceSynchronize());
+    if (s.precision == DGX_FP64) {
+        DGX_TRY_CUDA(cudaMemcpy(c, s.c, s.n * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<float> tmp(s.n);
+        DGX_TRY_CUDA(cudaMemcpy(tmp.data(), s.c, s.n * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < s.n; ++i) c[i] = tmp[i];
+    }
+    return DGX_OK;
+}
+
+int dgx_set_state_f32(dgx_solver *sv, const float *c, void *stream) {
+    if (!sv || !c) return DGX_ERR_INVALID;
+    SolverDev &s = sv->s;
+    if (s.precision != DGX_FP64) {
+        DGX_TRY_CUDA(cudaMemcpyAsync(s.c, c, s.n * sizeof(float), cudaMemcpyHostToDevice, as_stream(stream)));
+        return DGX_OK;
+    }
+    // stage through the accumulator buffer, then widen on the device
+    DGX_TRY_CUDA(cudaMemcpyAsync(s.acc, c, s.n * sizeof(float), cudaMemcpyHostToDevice, as_stream(stream)));
+    return convert_state(s.acc, 0, s.c, 1, s.n, as_stream(stream));
+}
+
+int dgx_get_state_f32(dgx_solver *sv, float *c, void *stream) {
+    if (!sv || !c) return DGX_ERR_INVALID;
+    SolverDev &s = sv->s;
+    if (s.precision != DGX_FP64) {
+        DGX_TRY_CUDA(cudaMemcpyAsync(c, s.c, s.n * sizeof(float), cudaMemcpyDeviceToHost, as_stream(stream)));
+        return DGX_OK;
+    }
+    int rc = convert_state(s.c, 1, s.acc, 0, s.n, as_stream(stream));
+    if (rc) return rc;
+    DGX_TRY_CUDA(cudaMemcpyAsync(c, s.acc, s.n * sizeof(float), cudaMemcpyDeviceToHost, as_stream(stream)));
+    return DGX_OK;
+}
+
+int dgx_state_device_ptr(dgx_solver *sv, void **ptr) {
+    if (!sv || !ptr) return DGX_ERR_INVALID;
+    *ptr = sv->s.c;
+    return DGX_OK;
+}
+
+int dgx_project_ic(dgx_solver *sv, int ic, const double *params) {
+    if (!sv) return DGX_ERR_INVALID;
+    if (ic < DGX_IC_GAUSSIAN || ic > DGX_IC_CONSTANT) { set_error("unknown initial condition %d", ic); return DGX_ERR_INVALID; }
+    if (sv->s.equation == DGX_EULER && (ic == DGX_IC_GAUSSIAN || ic == DGX_IC_POLY)) {
+        set_error("initial condition %d is scalar", ic);
+        return DGX_ERR_INVALID;
+    }
+    if (sv->s.equation == DGX_ADVECTION && (ic == DGX_IC_DENSITY_WAVE || ic == DGX_IC_VORTEX)) {
+        set_error("initial condition %d needs the Euler equations", ic);
+        return DGX_ERR_INVALID;
+    }
+    int rc = project_ic(sv->s, sv->mesh->d, ic, params, nullptr);
+    if (rc) return rc;
+    sv->launches++;
+    DGX_TRY_CUDA(cudaDeviceSynchronize());
+    return DGX_OK;
+}
+
+int dgx_rhs_eval(dgx_solver *sv, const void *u, void *k, double dt, double t, void *stream) {
+    if (!sv || !u || !k) return DGX_ERR_INVALID;
+    if (u == k) { set_error("u and k must not alias"); return DGX_ERR_INVALID; }
+    return stage_launch(sv, 0, u, nullptr, nullptr, k, dt, t, as_stream(stream));
+}
+
+int dgx_set_dt(dgx_solver *sv, int dt_mode, double dt, double cfl) {
+    if (!sv) return DGX_ERR_INVALID;
+    if (dt_mode != DGX_DT_FIXED && dt_mode != DGX_DT_CFL) { set_error("unknown dt mode"); return DGX_ERR_INVALID; }
+    if (dt_mode == DGX_DT_FIXED && !(dt > 0.0)) { set_error("fixed dt must be > 0"); return DGX_ERR_INVALID; }
+    if (dt_mode == DGX_DT_CFL && !(cfl > 0.0)) { set_error("cfl must be > 0"); return DGX_ERR_INVALID; }
+    sv->s.dt_mode = dt_mode;
+    int rc = write_scalar(sv->s, 3, dt_mode == DGX_DT_FIXED ? dt : 0.0);
+    if (!rc) rc = write_scalar(sv->s, 4, cfl);
+    return rc;
+}
+
+int dgx_set_end_time(dgx_solver *sv, double t_end) {
+    if (!sv) return DGX_ERR_INVALID;
+    return write_scalar(sv->s, 5, t_end);
+}
+
+int dgx_rk_stage(dgx_solver *sv, int stage, void *stream) {
+    if (!sv) return DGX_ERR_INVALID;
+    return run_stage(sv, stage, as_stream(stream));
+}
+
+int dgx_step(dgx_solver *sv, void *stream) {
+    if (!sv) return DGX_ERR_INVALID;
+    for (int st = 0; st < 4; ++st) {
+        int rc = run_stage(sv, st, as_stream(stream));
+        if (rc) return rc;
+    }
+    return DGX_OK;
+}
+
+int dgx_time(dgx_solver *sv, double *t, double *dt, void *stream) {
+    if (!sv) return DGX_ERR_INVALID;
+    double h[3];
+    DGX_TRY_CUDA(cudaMemcpyAsync(h, sv->s.scal, sizeof(h), cudaMemcpyDeviceToHost, as_stream(stream)));
+    DGX_TRY_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    if (t) *t = h[1];
+    if (dt) *dt = h[0];
+    return DGX_OK;
+}
+
+int dgx_reset_time(dgx_solver *sv, double t) {
+    if (!sv) return DGX_ERR_INVALID;
+    int rc = write_scalar(sv->s, 1, t);
+    if (!rc) rc = write_scalar(sv->s, 2, t);
+    if (!rc) rc = write_scalar(sv->s, 0, 0.0);
+    if (rc) return rc;
+    DGX_TRY_CUDA(cudaMemset(sv->s.steps, 0, sizeof(long long)));
+    DGX_TRY_CUDA(cudaMemset(sv->s.status, 0, sizeof(unsigned int)));
+    return DGX_OK;
+}
+
+int dgx_run(dgx_solver *sv, double t_end, int max_steps, int *steps, double *t, void *stream) {
+    if (!sv) return DGX_ERR_INVALID;
+    if (!(t_end > 0.0) && max_steps <= 0) { set_error("need t_end > 0 or max_steps > 0"); return DGX_ERR_INVALID; }
+    cudaStream_t st = as_stream(stream);
+    int rc = write_scalar(sv->s, 5, t_end > 0.0 ? t_end : 0.0);
+    if (rc) return rc;
+    long long s0 = 0, sn = 0;
+    DGX_TRY_CUDA(cudaMemcpy(&s0, sv->s.steps, sizeof(s0), cudaMemcpyDeviceToHost));
+    int issued = 0;
+    for (;;) {
+        int chunk = 16;
+        if (max_steps > 0 && max_steps - issued < chunk) chunk = max_steps - issued;
+        for (int i = 0; i < chunk; ++i) {
+            rc = dgx_step(sv, stream);
+            if (rc) return rc;
+        }
+        issued += chunk;
+        double h[2];
+        unsigned int status = 0;
+        DGX_TRY_CUDA(cudaMemcpyAsync(h, sv->s.scal, sizeof(h), cudaMemcpyDeviceToHost, st));
+        DGX_TRY_CUDA(cudaMemcpyAsync(&sn, sv->s.steps, sizeof(sn), cudaMemcpyDeviceToHost, st));
+        DGX_TRY_CUDA(cudaMemcpyAsync(&status, sv->s.status, sizeof(status), cudaMemcpyDeviceToHost, st));
+        DGX_TRY_CUDA(cudaStreamSynchronize(st));
+        if (status) { set_error("state became non-finite or unphysical (flags %u)", status); return DGX_ERR_NONFINITE; }
+        const bool done_t = t_end > 0.0 && (h[1] >= t_end || h[0] == 0.0);
+        const bool done_n = max_steps > 0 && issued >= max_steps;
+        if (done_t || done_n) {
+            if (steps) *steps = static_cast<int>(sn - s0);
+            if (t) *t = h[1];
+            return DGX_OK;
+        }
+    }
+}
+
+int dgx_conserved_totals(dgx_solver *sv, double *out, void *stream) {
+    if (!sv || !out) return DGX_ERR_INVALID;
+    int rc = conserved_totals(sv->s, sv->mesh->d, out, as_stream(stream));
+    if (!rc) sv->launches += 2 * sv->s.nv * 2;
+    return rc;
+}
+
+int dgx_max_wave_speed(dgx_solver *sv, double *out, void *stream) {
+    if (!sv || !out) return DGX_ERR_INVALID;
+    DGX_TRY_CUDA(cudaMemcpyAsync(out, sv->s.scal + 6, sizeof(double), cudaMemcpyDeviceToHost, as_stream(stream)));
+    DGX_TRY_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    return DGX_OK;
+}
+
+int dgx_launch_count(const dgx_solver *sv, long long *count) {
+    if (!sv || !count) return DGX_ERR_INVALID;
+    *count = sv->launches;
+    return DGX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,139 @@
+// dgx_internal.h -- handle layouts and helpers shared by the library's sources.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstddef>
+#include <cstdint>
+
+#include "dgx.h"
+#include "dgx_tables.h"
+
+namespace dgx {
+
+void set_error(const char *fmt, ...);
+
+#define DGX_TRY_CUDA(call)                                                                  \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) {                                                            \
+            ::dgx::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                             __LINE__);                                                     \
+            return DGX_ERR_CUDA;                                                            \
+        }                                                                                   \
+    } while (0)
+
+#define DGX_CHECK_LAUNCH()                                                                  \
+    do {                                                                                    \
+        cudaError_t e_ = cudaGetLastError();                                                \
+        if (e_ != cudaSuccess) {                                                            \
+            ::dgx::set_error("kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_),     \
+                             __FILE__, __LINE__);                                           \
+            return DGX_ERR_CUDA;                                                            \
+        }                                                                                   \
+    } while (0)
+
+// Bit flags of the per-solver device status word.
+enum StatusBits : unsigned int {
+    kStatusNonFinite = 1u,   // NaN/Inf wave speed or state
+    kStatusNegative = 2u,    // non-positive density or pressure in a cell average
+};
+
+// Element-side connectivity word: neighbour element e >= 0 packed as
+// e*8 + is_left*4 + neighbour's local side; a boundary side stores its
+// (negative) boundary tag.
+DGX_HD inline int pack_nbr(int e, int is_left, int side) { return e * 8 + is_left * 4 + side; }
+
+// Mesh geometry, computed in FP64 on the device at creation.
+struct MeshDev {
+    int num_elem = 0, num_sides = 0, num_boundary = 0;
+    // FP64 reference quantities (device)
+    double *V = nullptr;        // [6][E] V1x V1y V2x V2y V3x V3y
+    int *elem_s = nullptr;      // [3][E]
+    int *sides = nullptr;       // [4][S] left_elem right_elem left_side right_side
+    double *J = nullptr, *xr = nullptr, *yr = nullptr, *xs = nullptr, *ys = nullptr;
+    double *diam = nullptr;     // [E] inscribed diameters
+    double *len = nullptr, *nx = nullptr, *ny = nullptr;   // [S]
+    double min_diam = 0.0;
+    // per-element hot-path arrays
+    int *nbr = nullptr;         // [3][E] packed neighbour words
+    float *geo32 = nullptr;     // [5][E] 1/J, x_r, y_r, x_s, y_s
+    float *fn32 = nullptr;      // [3 sides][3][E] nx, ny, len/2 (normal out of the side's left element)
+    double *geo64 = nullptr;    // same in FP64
+    double *fn64 = nullptr;
+};
+
+}  // namespace dgx
+
+struct dgx_mesh {
+    dgx::MeshDev d;
+    int device = 0;
+    std::atomic<int> refs{1};
+};
+
+namespace dgx {
+
+struct SolverDev {
+    int order = 0, np = 0, nv = 0, equation = 0, flux = 0, precision = 0;
+    double gamma = 1.4, ax = 1.0, ay = 1.0;
+    size_t n = 0;                      // values per state vector
+    void *c = nullptr;                 // resident state (FP32 or FP64)
+    void *acc = nullptr;               // RK4 accumulator
+    void *ua = nullptr, *ub = nullptr; // stage inputs
+    // device scalars: [0] dt of the current step, [1] t at the end of it,
+    // [2] t at its start, [3] fixed dt, [4] cfl, [5] t_end, [6] max wave speed
+    double *scal = nullptr;
+    unsigned long long *lam_bits = nullptr;  // running max of the wave speed (double bits)
+    unsigned int *counter = nullptr;   // grid-completion counter of the CFL kernel
+    unsigned int *status = nullptr;    // StatusBits
+    long long *steps = nullptr;        // completed steps
+    double *red = nullptr;             // reduction scratch (partials)
+    int red_len = 0;
+    int dt_mode = DGX_DT_CFL;
+};
+
+}  // namespace dgx
+
+struct dgx_solver {
+    dgx_mesh *mesh = nullptr;
+    dgx::SolverDev s;
+    size_t device_bytes = 0;
+    long long launches = 0;
+};
+
+namespace dgx {
+
+// kernels/launchers implemented in the .cu sources
+int upload_tables_f32();
+int upload_tables_f64();
+int upload_tables_misc();
+
+struct StageArgs {
+    int E;
+    int mode;          // 0 rhs, 1..4 RK4 stages
+    int flux;
+    double gamma, ax, ay;
+    const void *u;     // stage input (read-only)
+    const void *c;     // base state
+    void *acc;         // accumulator
+    void *out;         // k (mode 0), next stage input (1..3), state (4)
+    const int *nbr;
+    const void *geo;
+    const void *fn;
+    const double *scal;   // device dt/t (modes 1..4); may be null for mode 0
+    double dt, t;         // host dt/t for mode 0
+};
+
+int launch_stage_f32(int order, int equation, const StageArgs &a, cudaStream_t st);
+int launch_stage_f64(int order, int equation, const StageArgs &a, cudaStream_t st);
+
+// misc kernels (dgx_misc.cu)
+int mesh_geometry(MeshDev &m, cudaStream_t st);
+int project_ic(const SolverDev &s, const MeshDev &m, int ic, const double *params, cudaStream_t st);
+int launch_dt(SolverDev &s, const MeshDev &m, cudaStream_t st);
+int conserved_totals(SolverDev &s, const MeshDev &m, double *out, cudaStream_t st);
+int convert_state(const void *src, int src_is_double, void *dst, int dst_is_double, size_t n,
+                  cudaStream_t st);
+
+}  // namespace dgx

@@ -1,0 +1,426 @@
+// dgx_misc.cu -- one-time and per-step support kernels: FP64 geometry,
+// initial-condition projection, the on-device CFL time step, deterministic
+// conserved-total reductions and state conversions.
+#include <cmath>
+#include <vector>
+
+#include "dgx_internal.h"
+
+namespace dgx {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+Tables *g_dev_tables[64] = {nullptr};   // FP64 tables per device, p = 0..kMaxOrder
+
+int dev_tables(const Tables **out) {
+    int dev = 0;
+    DGX_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) { set_error("device index out of range"); return DGX_ERR_UNSUPPORTED; }
+    if (!g_dev_tables[dev]) {
+        Tables host[kMaxOrder + 1];
+        for (int p = 0; p <= kMaxOrder; ++p) host[p] = tables(p);
+        Tables *d = nullptr;
+        DGX_TRY_CUDA(cudaMalloc(&d, sizeof(host)));
+        DGX_TRY_CUDA(cudaMemcpy(d, host, sizeof(host), cudaMemcpyHostToDevice));
+        g_dev_tables[dev] = d;
+    }
+    *out = g_dev_tables[dev];
+    return DGX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Geometry (FP64), src/2d/conservation/conserv_kernels.cu:338-514
+// ---------------------------------------------------------------------------
+__global__ void elem_geometry_kernel(MeshDev m) {
+    const int E = m.num_elem;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const size_t SE = E;
+    const double x1 = m.V[e], y1 = m.V[SE + e], x2 = m.V[2 * SE + e], y2 = m.V[3 * SE + e];
+    const double x3 = m.V[4 * SE + e], y3 = m.V[5 * SE + e];
+    const double J = (x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1);
+    m.J[e] = J;
+    m.xr[e] = x2 - x1; m.yr[e] = y2 - y1;
+    m.xs[e] = x3 - x1; m.ys[e] = y3 - y1;
+    // inscribed-circle diameter 2 area / semi-perimeter (Heron, :355-373)
+    const double a = hypot(x1 - x2, y1 - y2), b = hypot(x2 - x3, y2 - y3), c = hypot(x1 - x3, y1 - y3);
+    const double k = 0.5 * (a + b + c);
+    m.diam[e] = 2.0 * sqrt(k * (k - a) * (k - b) * (k - c)) / k;
+    m.geo32[e] = static_cast<float>(1.0 / J);
+    m.geo32[SE + e] = static_cast<float>(x2 - x1);
+    m.geo32[2 * SE + e] = static_cast<float>(y2 - y1);
+    m.geo32[3 * SE + e] = static_cast<float>(x3 - x1);
+    m.geo32[4 * SE + e] = static_cast<float>(y3 - y1);
+    m.geo64[e] = 1.0 / J;
+    m.geo64[SE + e] = x2 - x1;
+    m.geo64[2 * SE + e] = y2 - y1;
+    m.geo64[3 * SE + e] = x3 - x1;
+    m.geo64[4 * SE + e] = y3 - y1;
+}
+
+// length and unit normal of each side, from the left element's local side,
+// oriented away from the left element's opposite vertex (:410-498)
+__global__ void side_geometry_kernel(MeshDev m) {
+    const int S = m.num_sides;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const size_t SE = m.num_elem, SS = S;
+    const int L = m.sides[s], ls = m.sides[2 * SS + s];
+    const double px[3] = {m.V[L], m.V[2 * SE + L], m.V[4 * SE + L]};
+    const double py[3] = {m.V[SE + L], m.V[3 * SE + L], m.V[5 * SE + L]};
+    const int a = ls, b = (ls + 1) % 3, o = (ls + 2) % 3;
+    const double dx = px[b] - px[a], dy = py[b] - py[a];
+    const double len = hypot(dx, dy);
+    double nx = -dy / len, ny = dx / len;
+    const double tx = px[o] - 0.5 * (px[a] + px[b]), ty = py[o] - 0.5 * (py[a] + py[b]);
+    if (nx * tx + ny * ty > 0) { nx = -nx; ny = -ny; }
+    m.len[s] = len; m.nx[s] = nx; m.ny[s] = ny;
+}
+
+// element-side connectivity and side factors for the hot path
+__global__ void elem_side_kernel(MeshDev m) {
+    const int E = m.num_elem;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const size_t SE = E, SS = m.num_sides;
+    for (int k = 0; k < 3; ++k) {
+        const int s = m.elem_s[k * SE + e];
+        const int le = m.sides[s], re = m.sides[SS + s];
+        const int lsn = m.sides[2 * SS + s], rsn = m.sides[3 * SS + s];
+        const int il = (le == e) ? 1 : 0;   // the reference's rule (time_integrator.cu:153)
+        int word;
+        if (re < 0) word = re;
+        else word = il ? pack_nbr(re, 1, rsn) : pack_nbr(le, 0, lsn);
+        m.nbr[k * SE + e] = word;
+        m.fn32[(3 * k + 0) * SE + e] = static_cast<float>(m.nx[s]);
+        m.fn32[(3 * k + 1) * SE + e] = static_cast<float>(m.ny[s]);
+        m.fn32[(3 * k + 2) * SE + e] = static_cast<float>(0.5 * m.len[s]);
+        m.fn64[(3 * k + 0) * SE + e] = m.nx[s];
+        m.fn64[(3 * k + 1) * SE + e] = m.ny[s];
+        m.fn64[(3 * k + 2) * SE + e] = 0.5 * m.len[s];
+    }
+}
+
+// deterministic block reductions (fixed tree, fixed order of partials)
+template <int OP>   // 0 sum, 1 min
+__device__ double red_op(double a, double b) { return OP == 0 ? a + b : fmin(a, b); }
+
+template <int OP>
+__global__ void reduce_kernel(const double *x, size_t n, double *partial, double init) {
+    __shared__ double sh[kThreads];
+    double acc = init;
+    const size_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const size_t lo = blockIdx.x * chunk, hi = lo + chunk < n ? lo + chunk : n;
+    for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) acc = red_op<OP>(acc, x[i]);
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = kThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] = red_op<OP>(sh[threadIdx.x], sh[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// per-element products c_{n,0,e} * J_e for the conserved totals
+template <typename T>
+__global__ void mass_terms_kernel(const T *c, const double *J, int E, int np, int n, double *out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < E) out[e] = static_cast<double>(c[static_cast<size_t>(n) * np * E + e]) * J[e];
+}
+
+// ---------------------------------------------------------------------------
+// Initial conditions (FP64), conserv_kernels.cu:167-187, euler.cu:31-59
+// ---------------------------------------------------------------------------
+__device__ double wrap_dist(double d, double L) {
+    if (L > 0) {
+        d = fmod(d, L);
+        if (d > 0.5 * L) d -= L;
+        if (d < -0.5 * L) d += L;
+    }
+    return d;
+}
+
+__device__ void ic_eval(int ic, const double *P, double g, double x, double y, double *U) {
+    const double pi = 3.14159265358979323846;
+    switch (ic) {
+    case DGX_IC_GAUSSIAN: {
+        const double dx = wrap_dist(x - P[0], P[3]), dy = wrap_dist(y - P[1], P[4]);
+        U[0] = exp(-(dx * dx + dy * dy) / P[2]);
+        break;
+    }
+    case DGX_IC_POLY: U[0] = pow(x - y, P[0]); break;
+    case DGX_IC_DENSITY_WAVE: {
+        const double rho = 1.0 + P[0] * sin(2.0 * pi * P[4] * (x + y));
+        U[0] = rho; U[1] = rho * P[1]; U[2] = rho * P[2];
+        U[3] = P[3] / (g - 1.0) + 0.5 * rho * (P[1] * P[1] + P[2] * P[2]);
+        break;
+    }
+    case DGX_IC_VORTEX: {
+        const double dx = wrap_dist(x - P[0], P[5]), dy = wrap_dist(y - P[1], P[6]);
+        const double r2 = dx * dx + dy * dy, b = P[2];
+        const double f = exp(0.5 * (1.0 - r2));
+        const double u = P[3] - b / (2.0 * pi) * f * dy;
+        const double v = P[4] + b / (2.0 * pi) * f * dx;
+        const double T = 1.0 - (g - 1.0) * b * b / (8.0 * g * pi * pi) * f * f;
+        const double rho = pow(T, 1.0 / (g - 1.0)), p = pow(rho, g);
+        U[0] = rho; U[1] = rho * u; U[2] = rho * v;
+        U[3] = p / (g - 1.0) + 0.5 * rho * (u * u + v * v);
+        break;
+    }
+    default:
+        U[0] = P[0]; U[1] = P[0] * P[1]; U[2] = P[0] * P[2];
+        U[3] = P[3] / (g - 1.0) + 0.5 * P[0] * (P[1] * P[1] + P[2] * P[2]);
+        break;
+    }
+}
+
+struct IcArgs { double P[8]; };
+
+template <typename T>
+__global__ void project_kernel(MeshDev m, const Tables *tabs, int p, int nv, int ic, IcArgs A,
+                               double g, T *c) {
+    const int E = m.num_elem;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const Tables &Tb = tabs[p];
+    const size_t SE = E;
+    const double v1x = m.V[e], v1y = m.V[SE + e], v2x = m.V[2 * SE + e], v2y = m.V[3 * SE + e];
+    const double v3x = m.V[4 * SE + e], v3y = m.V[5 * SE + e];
+    double acc[4][kMaxModes];
+    for (int n = 0; n < 4; ++n)
+        for (int i = 0; i < Tb.np; ++i) acc[n][i] = 0.0;
+    for (int q = 0; q < Tb.nq; ++q) {
+        const double r = Tb.r1[q], s = Tb.r2[q];
+        const double x = r * v2x + s * v3x + (1 - r - s) * v1x;
+        const double y = r * v2y + s * v3y + (1 - r - s) * v1y;
+        double U[4];
+        ic_eval(ic, A.P, g, x, y, U);
+        for (int i = 0; i < Tb.np; ++i)
+            for (int n = 0; n < nv; ++n) acc[n][i] += Tb.w[q] * U[n] * Tb.phi[i * Tb.nq + q];
+    }
+    for (int n = 0; n < nv; ++n)
+        for (int i = 0; i < Tb.np; ++i) c[(static_cast<size_t>(n) * Tb.np + i) * SE + e] = static_cast<T>(acc[n][i]);
+}
+
+// ---------------------------------------------------------------------------
+// Time step: per-step maximum cell-average wave speed (euler.cu:252-278) and
+// dt = cfl * min diameter / lambda / (2p+1), clipped at t_end
+// (time_integrator.cu:252-270).  The last block to finish computes dt, so the
+// whole step stays on the device.
+// ---------------------------------------------------------------------------
+struct DtArgs {
+    const void *c;
+    int E, np, is_double, euler, cfl_mode, order;
+    double gamma, phi0, amax, min_diam;
+    double *scal;
+    unsigned long long *lam_bits;
+    unsigned int *counter, *status;
+    long long *steps;
+};
+
+__device__ void finish_dt(const DtArgs &a, double lam) {
+    double *sc = a.scal;
+    const double t = sc[1], t_end = sc[5];
+    double dt;
+    if (a.cfl_mode) dt = sc[4] * a.min_diam / lam / (2.0 * a.order + 1.0);
+    else dt = sc[3];
+    if (!(lam == lam) || !(dt > 0.0) || !isfinite(dt)) {   // NaN state or no progress possible
+        atomicOr(a.status, kStatusNonFinite);
+        dt = 0.0;
+    }
+    double tn = t + dt;
+    if (t_end > 0.0) {
+        if (t >= t_end) { dt = 0.0; tn = t; }
+        else if (t + dt > t_end) { dt = t_end - t; tn = t_end; }
+    }
+    sc[0] = dt;
+    sc[2] = t;
+    sc[1] = tn;
+    sc[6] = lam;
+    if (dt > 0.0) *a.steps += 1;
+}
+
+template <typename T>
+__global__ void cfl_kernel(DtArgs a) {
+    __shared__ double sh[kThreads / 32];
+    double lmax = 0.0;
+    unsigned int bad = 0;
+    if (a.euler) {
+        const T *c = static_cast<const T *>(a.c);
+        const size_t SE = a.E, NPE = static_cast<size_t>(a.np) * SE;
+        for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.E; e += gridDim.x * blockDim.x) {
+            const double rho = static_cast<double>(c[e]) * a.phi0;
+            const double ru = static_cast<double>(c[NPE + e]) * a.phi0;
+            const double rv = static_cast<double>(c[2 * NPE + e]) * a.phi0;
+            const double E = static_cast<double>(c[3 * NPE + e]) * a.phi0;
+            const double p = (a.gamma - 1.0) * (E - (ru * ru + rv * rv) / 2.0 / rho);
+            if (!(rho > 0.0) || !(p > 0.0)) bad |= kStatusNegative;
+            const double cs = sqrt(a.gamma * p / rho);
+            const double sp = sqrt(ru * ru + rv * rv) / rho;
+            const double lam = sp + cs;
+            if (!(lam == lam)) bad |= kStatusNonFinite;
+            else lmax = fmax(lmax, lam);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = lmax;
+    if (bad) atomicOr(a.status, bad);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) m = fmax(m, sh[w]);
+        // non-negative doubles order like their bit patterns
+        atomicMax(a.lam_bits, static_cast<unsigned long long>(__double_as_longlong(m)));
+        __threadfence();
+        const unsigned int done = atomicAdd(a.counter, 1u);
+        if (done == gridDim.x - 1) {
+            __threadfence();
+            const double lam = a.euler ? __longlong_as_double(static_cast<long long>(atomicAdd(a.lam_bits, 0ull)))
+                                       : a.amax;
+            const unsigned int st = atomicAdd(a.status, 0u);
+            finish_dt(a, st ? __longlong_as_double(0x7ff8000000000000ll) : lam);
+            *a.lam_bits = 0ull;
+            *a.counter = 0u;
+        }
+    }
+}
+
+template <typename T>
+__global__ void convert_kernel(const void *src, int src_double, T *dst, size_t n) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x)
+        dst[i] = src_double ? static_cast<T>(static_cast<const double *>(src)[i])
+                            : static_cast<T>(static_cast<const float *>(src)[i]);
+}
+
+int blocks_for(size_t n) { return static_cast<int>((n + kThreads - 1) / kThreads); }
+
+// deterministic reduction of x[0..n) with a fixed grid; result to *host
+int reduce_host(const double *x, size_t n, int op, double *scratch, int scratch_len, double *host,
+                cudaStream_t st) {
+    int grid = static_cast<int>((n + kThreads - 1) / kThreads);
+    if (grid > scratch_len) grid = scratch_len;
+    if (grid < 1) grid = 1;
+    if (op == 0) reduce_kernel<0><<<grid, kThreads, 0, st>>>(x, n, scratch, 0.0);
+    else reduce_kernel<1><<<grid, kThreads, 0, st>>>(x, n, scratch, INFINITY);
+    DGX_CHECK_LAUNCH();
+    if (op == 0) reduce_kernel<0><<<1, kThreads, 0, st>>>(scratch, grid, scratch + scratch_len, 0.0);
+    else reduce_kernel<1><<<1, kThreads, 0, st>>>(scratch, grid, scratch + scratch_len, INFINITY);
+    DGX_CHECK_LAUNCH();
+    DGX_TRY_CUDA(cudaMemcpyAsync(host, scratch + scratch_len, sizeof(double), cudaMemcpyDeviceToHost, st));
+    DGX_TRY_CUDA(cudaStreamSynchronize(st));
+    return DGX_OK;
+}
+
+}  // namespace
+
+int upload_tables_misc() {
+    const Tables *t = nullptr;
+    return dev_tables(&t);
+}
+
+int mesh_geometry(MeshDev &m, cudaStream_t st) {
+    const int E = m.num_elem, S = m.num_sides;
+    elem_geometry_kernel<<<blocks_for(E), kThreads, 0, st>>>(m);
+    DGX_CHECK_LAUNCH();
+    side_geometry_kernel<<<blocks_for(S), kThreads, 0, st>>>(m);
+    DGX_CHECK_LAUNCH();
+    elem_side_kernel<<<blocks_for(E), kThreads, 0, st>>>(m);
+    DGX_CHECK_LAUNCH();
+    // minimum inscribed diameter (exact: min is order independent)
+    const int len = 4096;
+    double *scratch = nullptr;
+    DGX_TRY_CUDA(cudaMalloc(&scratch, sizeof(double) * (len + 1)));
+    int rc = reduce_host(m.diam, E, 1, scratch, len, &m.min_diam, st);
+    cudaFree(scratch);
+    return rc;
+}
+
+int project_ic(const SolverDev &s, const MeshDev &m, int ic, const double *params, cudaStream_t st) {
+    const Tables *tabs = nullptr;
+    int rc = dev_tables(&tabs);
+    if (rc) return rc;
+    IcArgs A;
+    for (int i = 0; i < 8; ++i) A.P[i] = params ? params[i] : 0.0;
+    if (s.precision == DGX_FP64)
+        project_kernel<double><<<blocks_for(m.num_elem), kThreads, 0, st>>>(
+            m, tabs, s.order, s.nv, ic, A, s.gamma, static_cast<double *>(s.c));
+    else
+        project_kernel<float><<<blocks_for(m.num_elem), kThreads, 0, st>>>(
+            m, tabs, s.order, s.nv, ic, A, s.gamma, static_cast<float *>(s.c));
+    DGX_CHECK_LAUNCH();
+    return DGX_OK;
+}
+
+int launch_dt(SolverDev &s, const MeshDev &m, cudaStream_t st) {
+    DtArgs a;
+    a.c = s.c;
+    a.E = m.num_elem;
+    a.np = s.np;
+    a.is_double = s.precision == DGX_FP64;
+    a.euler = s.equation == DGX_EULER && s.dt_mode == DGX_DT_CFL;
+    a.cfl_mode = s.dt_mode == DGX_DT_CFL;
+    a.order = s.order;
+    a.gamma = s.gamma;
+    a.phi0 = tables(s.order).phi[0];
+    a.amax = std::sqrt(s.ax * s.ax + s.ay * s.ay);
+    a.min_diam = m.min_diam;
+    a.scal = s.scal;
+    a.lam_bits = s.lam_bits;
+    a.counter = s.counter;
+    a.status = s.status;
+    a.steps = s.steps;
+    int grid = 1;
+    if (a.euler) {
+        grid = blocks_for(m.num_elem);
+        if (grid > 152 * 8) grid = 152 * 8;
+    }
+    if (a.is_double) cfl_kernel<double><<<grid, kThreads, 0, st>>>(a);
+    else cfl_kernel<float><<<grid, kThreads, 0, st>>>(a);
+    DGX_CHECK_LAUNCH();
+    return DGX_OK;
+}
+
+int conserved_totals(SolverDev &s, const MeshDev &m, double *out, cudaStream_t st) {
+    const int E = m.num_elem;
+    double *terms = nullptr;
+    const int len = 4096;
+    double *scratch = nullptr;
+    DGX_TRY_CUDA(cudaMalloc(&terms, sizeof(double) * E));
+    if (cudaMalloc(&scratch, sizeof(double) * (len + 1)) != cudaSuccess) {
+        cudaFree(terms);
+        set_error("cudaMalloc failed");
+        return DGX_ERR_NOMEM;
+    }
+    const double phi0 = tables(s.order).phi[0];
+    int rc = DGX_OK;
+    for (int n = 0; n < s.nv && rc == DGX_OK; ++n) {
+        if (s.precision == DGX_FP64)
+            mass_terms_kernel<double><<<blocks_for(E), kThreads, 0, st>>>(
+                static_cast<const double *>(s.c), m.J, E, s.np, n, terms);
+        else
+            mass_terms_kernel<float><<<blocks_for(E), kThreads, 0, st>>>(
+                static_cast<const float *>(s.c), m.J, E, s.np, n, terms);
+        if (cudaGetLastError() != cudaSuccess) { rc = DGX_ERR_CUDA; break; }
+        double sum = 0.0;
+        rc = reduce_host(terms, E, 0, scratch, len, &sum, st);
+        out[n] = sum * phi0 * 0.5;
+    }
+    cudaFree(terms);
+    cudaFree(scratch);
+    return rc;
+}
+
+int convert_state(const void *src, int src_is_double, void *dst, int dst_is_double, size_t n,
+                  cudaStream_t st) {
+    int grid = blocks_for(n);
+    if (grid > 152 * 16) grid = 152 * 16;
+    if (dst_is_double) convert_kernel<double><<<grid, kThreads, 0, st>>>(src, src_is_double, static_cast<double *>(dst), n);
+    else convert_kernel<float><<<grid, kThreads, 0, st>>>(src, src_is_double, static_cast<float *>(dst), n);
+    DGX_CHECK_LAUNCH();
+    return DGX_OK;
+}
+
+}  // namespace dgx

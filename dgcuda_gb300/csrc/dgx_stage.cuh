@@ -1,0 +1,339 @@
+// dgx_stage.cuh -- the fused RHS / RK-stage kernel, one thread per element.
+//
+// Included by dgx_stage_f32.cu and dgx_stage_f64.cu with DGX_REAL defined as
+// the arithmetic type.  Each translation unit owns its copy of the constant
+// tables (uploaded by upload_tables_f32/_f64).
+//
+// Per element e the kernel computes, in registers,
+//   volume   V_i = sum_q gx_iq (Fx ys - Fy xs) + gy_iq (Fy xr - Fx yr)      at U(q)
+//            (src/2d/conservation/conserv_kernels.cu:766-811)
+//   surface  for each local side k: own trace and neighbour trace at the p+1
+//            Gauss points (the neighbour's points in reverse order), the
+//            numerical flux Fhat(U_left, U_right, n_left) and the lift
+//            -+ len/2 sum_j w_j Fhat_j phi_i(j)  (conserv_kernels.cu:697-758)
+//   rhs      k = dt/J (V + sum of the three sides), sides in local order
+//            0,1,2 (time_integrator.cu:130-188)
+// and fuses the RK4 combination of the stage (time_integrator.cu:194-218).
+// The flux of a side is evaluated by both of its elements with the same
+// arguments (left trace, right trace, left normal) and the same instruction
+// sequence, so the two evaluations agree bit for bit; there are no atomics and
+// the result does not depend on scheduling.
+#pragma once
+
+#include "dgx_internal.h"
+
+#ifndef DGX_REAL
+#error "define DGX_REAL before including dgx_stage.cuh"
+#endif
+
+namespace dgx {
+
+constexpr int kStageThreads = 128;
+
+static __constant__ DGX_REAL c_tab[kTableTotal];
+
+template <int P>
+struct Lay {
+    static constexpr int NP = num_modes(P), NQ = num_quad(P), NQ1 = num_quad1(P);
+    static constexpr int PHI = table_offset(P);
+    static constexpr int GX = PHI + NP * NQ;
+    static constexpr int GY = GX + NP * NQ;
+    static constexpr int SIDE = GY + NP * NQ;
+    static constexpr int LIFT = SIDE + 3 * NP * NQ1;
+    static constexpr int W1 = LIFT + 3 * NP * NQ1;
+};
+
+using R = DGX_REAL;
+
+__device__ __forceinline__ R rrcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ R rrcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ R rsqrt_(float x) { return sqrtf(x); }
+__device__ __forceinline__ R rsqrt_(double x) { return sqrt(x); }
+
+// Physical flux (Fx, Fy) at a point: advection a*u, Euler
+// (src/2d/conservation/euler/euler.cu:92-117).
+template <int EQ>
+__device__ __forceinline__ void phys_flux(const R *U, R g, R ax, R ay, R *fx, R *fy) {
+    if constexpr (EQ == DGX_ADVECTION) {
+        fx[0] = ax * U[0];
+        fy[0] = ay * U[0];
+    } else {
+        const R ir = rrcp(U[0]);
+        const R u = U[1] * ir, v = U[2] * ir;
+        const R p = (g - R(1)) * (U[3] - R(0.5) * (U[1] * u + U[2] * v));
+        fx[0] = U[1];         fy[0] = U[2];
+        fx[1] = U[1] * u + p; fy[1] = U[1] * v;
+        fx[2] = U[2] * u;     fy[2] = U[2] * v + p;
+        fx[3] = (U[3] + p) * u;
+        fy[3] = (U[3] + p) * v;
+    }
+}
+
+// Numerical flux Fhat . n with n oriented out of the left element:
+// 1/2 [ (F(UL) + F(UR)) . n + lambda (UL - UR) ] with the local Lax-Friedrichs
+// lambda = max(|u_n| + c) over both sides (euler.cu:127-168), lambda = |a.n| for
+// advection; lambda = 0 for the central flux (2dadvec_kernels.cu:162-164).
+template <int EQ>
+__device__ __forceinline__ void num_flux(const R *UL, const R *UR, R nx, R ny, int llf, R g,
+                                         R ax, R ay, R *Fh) {
+    if constexpr (EQ == DGX_ADVECTION) {
+        const R an = ax * nx + ay * ny;
+        const R lam = llf ? fabs(an) : R(0);
+        Fh[0] = R(0.5) * (an * (UL[0] + UR[0]) + lam * (UL[0] - UR[0]));
+    } else {
+        const R irl = rrcp(UL[0]), irr = rrcp(UR[0]);
+        const R ul = UL[1] * irl, vl = UL[2] * irl, ur = UR[1] * irr, vr = UR[2] * irr;
+        const R pl = (g - R(1)) * (UL[3] - R(0.5) * (UL[1] * ul + UL[2] * vl));
+        const R pr = (g - R(1)) * (UR[3] - R(0.5) * (UR[1] * ur + UR[2] * vr));
+        const R unl = ul * nx + vl * ny, unr = ur * nx + vr * ny;
+        R lam = R(0);
+        if (llf) {
+            const R ll = fabs(unl) + rsqrt_(g * pl * irl);
+            const R lr = fabs(unr) + rsqrt_(g * pr * irr);
+            lam = ll > lr ? ll : lr;
+        }
+        const R fl[4] = {UL[1] * nx + UL[2] * ny, UL[1] * unl + pl * nx, UL[2] * unl + pl * ny,
+                         (UL[3] + pl) * unl};
+        const R fr[4] = {UR[1] * nx + UR[2] * ny, UR[1] * unr + pr * nx, UR[2] * unr + pr * ny,
+                         (UR[3] + pr) * unr};
+#pragma unroll
+        for (int n = 0; n < 4; ++n) Fh[n] = R(0.5) * ((fl[n] + fr[n]) + lam * (UL[n] - UR[n]));
+    }
+}
+
+template <int P, int EQ>
+__global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageArgs a) {
+    using L = Lay<P>;
+    constexpr int NP = L::NP, NQ = L::NQ, NQ1 = L::NQ1;
+    constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
+    __shared__ R s_side[3 * NP * NQ1];
+    for (int t = threadIdx.x; t < 3 * NP * NQ1; t += blockDim.x) s_side[t] = c_tab[L::SIDE + t];
+    __syncthreads();
+
+    const int E = a.E;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    R dt;
+    if (a.mode == 0) {
+        dt = R(a.dt);
+    } else {
+        dt = R(a.scal[0]);
+        if (dt == R(0)) return;   // the run has reached its end time
+    }
+    const size_t SE = static_cast<size_t>(E);
+    const R g = R(a.gamma), ax = R(a.ax), ay = R(a.ay);
+    const int llf = a.flux == DGX_FLUX_LLF;
+    const R *__restrict__ u = static_cast<const R *>(a.u);
+
+    R c[NV][NP];
+#pragma unroll
+    for (int n = 0; n < NV; ++n)
+#pragma unroll
+        for (int i = 0; i < NP; ++i) c[n][i] = __ldg(u + (n * NP + i) * SE + e);
+
+    const R *__restrict__ geo = static_cast<const R *>(a.geo);
+    const R invJ = __ldg(geo + e), xr = __ldg(geo + SE + e), yr = __ldg(geo + 2 * SE + e);
+    const R xs = __ldg(geo + 3 * SE + e), ys = __ldg(geo + 4 * SE + e);
+
+    R rhs[NV][NP];
+#pragma unroll
+    for (int n = 0; n < NV; ++n)
+#pragma unroll
+        for (int i = 0; i < NP; ++i) rhs[n][i] = R(0);
+
+    // ---- volume integral ------------------------------------------------------
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        R U[NV], fx[NV], fy[NV];
+#pragma unroll
+        for (int n = 0; n < NV; ++n) {
+            R s = R(0);
+#pragma unroll
+            for (int i = 0; i < NP; ++i) s = fma(c[n][i], c_tab[L::PHI + i * NQ + q], s);
+            U[n] = s;
+        }
+        phys_flux<EQ>(U, g, ax, ay, fx, fy);
+#pragma unroll
+        for (int n = 0; n < NV; ++n) {
+            const R hr = fx[n] * ys - fy[n] * xs;
+            const R hs = fy[n] * xr - fx[n] * yr;
+#pragma unroll
+            for (int i = 0; i < NP; ++i)
+                rhs[n][i] = fma(c_tab[L::GX + i * NQ + q], hr, fma(c_tab[L::GY + i * NQ + q], hs, rhs[n][i]));
+        }
+    }
+
+    // ---- the three sides ----------------------------------------------------
+    const int *__restrict__ nbr = a.nbr;
+    const R *__restrict__ fn = static_cast<const R *>(a.fn);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int nb = __ldg(nbr + k * SE + e);
+        const R nx = __ldg(fn + (3 * k + 0) * SE + e);
+        const R ny = __ldg(fn + (3 * k + 1) * SE + e);
+        const R hl = __ldg(fn + (3 * k + 2) * SE + e);
+        R UO[NQ1][NV], UN[NQ1][NV];
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j)
+#pragma unroll
+            for (int n = 0; n < NV; ++n) {
+                R s = R(0);
+#pragma unroll
+                for (int i = 0; i < NP; ++i) s = fma(c[n][i], c_tab[L::SIDE + (k * NP + i) * NQ1 + j], s);
+                UO[j][n] = s;
+            }
+        int il = 1;
+        if (nb >= 0) {
+            const int ne = nb >> 3, ns = nb & 3;
+            il = (nb >> 2) & 1;
+            R cn[NV][NP];
+#pragma unroll
+            for (int n = 0; n < NV; ++n)
+#pragma unroll
+                for (int i = 0; i < NP; ++i) cn[n][i] = __ldg(u + (n * NP + i) * SE + ne);
+            const R *ts = s_side + ns * NP * NQ1;
+#pragma unroll
+            for (int j = 0; j < NQ1; ++j)
+#pragma unroll
+                for (int n = 0; n < NV; ++n) {
+                    R s = R(0);
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) s = fma(cn[n][i], ts[i * NQ1 + (NQ1 - 1 - j)], s);
+                    UN[j][n] = s;
+                }
+        } else {
+            // boundary sides are rejected at solver creation; mirror state
+#pragma unroll
+            for (int j = 0; j < NQ1; ++j)
+#pragma unroll
+                for (int n = 0; n < NV; ++n) UN[j][n] = UO[j][n];
+        }
+        R Fh[NQ1][NV];
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j) {
+            R UL[NV], UR[NV];
+#pragma unroll
+            for (int n = 0; n < NV; ++n) {
+                UL[n] = il ? UO[j][n] : UN[j][n];
+                UR[n] = il ? UN[j][n] : UO[j][n];
+            }
+            num_flux<EQ>(UL, UR, nx, ny, llf, g, ax, ay, Fh[j]);
+        }
+        const R sg = il ? -hl : hl;
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                R s = R(0);
+#pragma unroll
+                for (int j = 0; j < NQ1; ++j) s = fma(c_tab[L::LIFT + (k * NP + i) * NQ1 + j], Fh[j][n], s);
+                rhs[n][i] = fma(sg, s, rhs[n][i]);
+            }
+    }
+
+    // ---- mass inverse and RK combination ---------------------------------------
+    const R sc = dt * invJ;
+    R *__restrict__ out = static_cast<R *>(a.out);
+    switch (a.mode) {
+    case 0:
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) out[(n * NP + i) * SE + e] = sc * rhs[n][i];
+        break;
+    case 1: {   // u2 = c + k1/2, acc = c + k1/6
+        R *__restrict__ acc = static_cast<R *>(a.acc);
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const R kk = sc * rhs[n][i];
+                const size_t o = (n * NP + i) * SE + e;
+                out[o] = fma(R(0.5), kk, c[n][i]);
+                acc[o] = fma(R(1.0 / 6.0), kk, c[n][i]);
+            }
+        break;
+    }
+    case 2:     // u3 = c + k2/2, acc += k2/3
+    case 3: {   // u4 = c + k3,   acc += k3/3
+        const R *__restrict__ cb = static_cast<const R *>(a.c);
+        R *__restrict__ acc = static_cast<R *>(a.acc);
+        const R alpha = a.mode == 2 ? R(0.5) : R(1);
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const R kk = sc * rhs[n][i];
+                const size_t o = (n * NP + i) * SE + e;
+                out[o] = fma(alpha, kk, __ldg(cb + o));
+                acc[o] = fma(R(1.0 / 3.0), kk, acc[o]);
+            }
+        break;
+    }
+    default: {  // c = acc + k4/6
+        const R *__restrict__ acc = static_cast<const R *>(a.acc);
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const size_t o = (n * NP + i) * SE + e;
+                out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], acc[o]);
+            }
+        break;
+    }
+    }
+}
+
+template <int P, int EQ>
+static int launch_one(const StageArgs &a, cudaStream_t st) {
+    const int grid = (a.E + kStageThreads - 1) / kStageThreads;
+    if (grid > 0) stage_kernel<P, EQ><<<grid, kStageThreads, 0, st>>>(a);
+    DGX_CHECK_LAUNCH();
+    return DGX_OK;
+}
+
+template <int EQ>
+static int launch_order(int order, const StageArgs &a, cudaStream_t st) {
+    switch (order) {
+    case 0: return launch_one<0, EQ>(a, st);
+    case 1: return launch_one<1, EQ>(a, st);
+    case 2: return launch_one<2, EQ>(a, st);
+    case 3: return launch_one<3, EQ>(a, st);
+    case 4: return launch_one<4, EQ>(a, st);
+    case 5: return launch_one<5, EQ>(a, st);
+    default: set_error("unsupported order %d", order); return DGX_ERR_UNSUPPORTED;
+    }
+}
+
+static int launch_stage_impl(int order, int equation, const StageArgs &a, cudaStream_t st) {
+    return equation == DGX_EULER ? launch_order<DGX_EULER>(order, a, st)
+                                 : launch_order<DGX_ADVECTION>(order, a, st);
+}
+
+// Fill this translation unit's constant tables from the FP64 host tables.
+static int upload_tables_impl() {
+    static R host[kTableTotal];
+    for (int p = 0; p <= kMaxOrder; ++p) {
+        const Tables &T = tables(p);
+        const int np = T.np, nq = T.nq, nq1 = T.nq1;
+        R *b = host + table_offset(p);
+        for (int i = 0; i < np * nq; ++i) {
+            b[i] = static_cast<R>(T.phi[i]);
+            b[np * nq + i] = static_cast<R>(T.gx[i]);
+            b[2 * np * nq + i] = static_cast<R>(T.gy[i]);
+        }
+        R *sd = b + 3 * np * nq, *lf = sd + 3 * np * nq1, *w1 = lf + 3 * np * nq1;
+        for (int sdi = 0; sdi < 3; ++sdi)
+            for (int i = 0; i < np; ++i)
+                for (int j = 0; j < nq1; ++j) {
+                    const int o = (sdi * np + i) * nq1 + j;
+                    sd[o] = static_cast<R>(T.side[o]);
+                    lf[o] = static_cast<R>(T.w1[j] * T.side[o]);
+                }
+        for (int j = 0; j < nq1; ++j) w1[j] = static_cast<R>(T.w1[j]);
+    }
+    DGX_TRY_CUDA(cudaMemcpyToSymbol(c_tab, host, sizeof(host)));
+    return DGX_OK;
+}
+
+}  // namespace dgx

@@ -1,0 +1,243 @@
+"""Triangle meshes in the reference's array layout.
+
+A mesh is the set of arrays the reference's driver builds from a ``.pmsh`` file
+(``read_mesh``, src/2d/conservation/conserv.cu:118-192):
+
+* ``V1x, V1y, V2x, V2y, V3x, V3y`` -- the three vertices of each element,
+  counter-clockwise (positive Jacobian), float64 ``[num_elem]``;
+* ``elem_s1, elem_s2, elem_s3`` -- the side index of the element's local sides
+  0 (V1->V2), 1 (V2->V3) and 2 (V3->V1), int32 ``[num_elem]``;
+* ``left_elem, right_elem`` -- the two elements of each side; ``right_elem < 0``
+  marks a boundary side (-1 reflecting, -2 outflow, -3 inflow,
+  conserv_kernels.cu:657-679), int32 ``[num_sides]``;
+* ``left_side, right_side`` -- the local side number of the side in the left
+  and right element, int32 ``[num_sides]``.
+
+Periodic meshes pair the sides on opposite boundaries as ordinary interior
+sides, so they carry no boundary tags.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+__all__ = ["Mesh", "periodic_square", "scramble", "dirichlet_square"]
+
+
+@dataclass
+class Mesh:
+    V1x: np.ndarray
+    V1y: np.ndarray
+    V2x: np.ndarray
+    V2y: np.ndarray
+    V3x: np.ndarray
+    V3y: np.ndarray
+    elem_s1: np.ndarray
+    elem_s2: np.ndarray
+    elem_s3: np.ndarray
+    left_elem: np.ndarray
+    right_elem: np.ndarray
+    left_side: np.ndarray
+    right_side: np.ndarray
+    meta: dict = field(default_factory=dict)
+
+    def __post_init__(self):
+        for k in ("V1x", "V1y", "V2x", "V2y", "V3x", "V3y"):
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.float64))
+        for k in ("elem_s1", "elem_s2", "elem_s3", "left_elem", "right_elem",
+                  "left_side", "right_side"):
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.int32))
+
+    @property
+    def num_elem(self) -> int:
+        return int(self.V1x.shape[0])
+
+    @property
+    def num_sides(self) -> int:
+        return int(self.left_elem.shape[0])
+
+    def vertices(self):
+        return (self.V1x, self.V1y, self.V2x, self.V2y, self.V3x, self.V3y)
+
+    def elem_sides(self):
+        return (self.elem_s1, self.elem_s2, self.elem_s3)
+
+    def side_arrays(self):
+        return (self.left_elem, self.right_elem, self.left_side, self.right_side)
+
+    def jacobian(self) -> np.ndarray:
+        return ((self.V2x - self.V1x) * (self.V3y - self.V1y)
+                - (self.V3x - self.V1x) * (self.V2y - self.V1y))
+
+    def centroids(self):
+        return ((self.V1x + self.V2x + self.V3x) / 3.0,
+                (self.V1y + self.V2y + self.V3y) / 3.0)
+
+    def check(self) -> None:
+        """Raise ValueError if the connectivity is inconsistent."""
+        E, S = self.num_elem, self.num_sides
+        es = np.stack(self.elem_sides(), axis=1)
+        if es.min() < 0 or es.max() >= S:
+            raise ValueError("elem_s out of range")
+        if self.left_elem.min() < 0 or self.left_elem.max() >= E:
+            raise ValueError("left_elem out of range")
+        if self.right_elem.max() >= E:
+            raise ValueError("right_elem out of range")
+        if np.any(self.jacobian() <= 0):
+            raise ValueError("elements must be counter-clockwise")
+        for s_arr, e_arr, name in ((self.left_side, self.left_elem, "left"),
+                                   (self.right_side, self.right_elem, "right")):
+            interior = e_arr >= 0
+            if np.any((s_arr[interior] < 0) | (s_arr[interior] > 2)):
+                raise ValueError(f"{name}_side out of range")
+            ok = es[e_arr[interior], s_arr[interior]] == np.nonzero(interior)[0]
+            if not np.all(ok):
+                raise ValueError(f"{name} side numbers disagree with elem_s")
+
+
+def periodic_square(n: int, lx: float = 1.0, ly: float = 1.0, x0: float = 0.0,
+                    y0: float = 0.0, jitter: float = 0.0, seed: int = 0) -> Mesh:
+    """Structured periodic triangulation of [x0,x0+lx] x [y0,y0+ly].
+
+    ``n x n`` squares, each split along its SW-NE diagonal into a lower
+    triangle (SW, SE, NE) and an upper triangle (SW, NE, NW): ``2 n^2``
+    elements and ``3 n^2`` sides.  Interior vertices move by independent
+    uniform offsets in ``[-jitter h, +jitter h]`` (seeded); boundary vertices
+    stay put so that periodic images coincide.  Element ``2q`` and ``2q+1``
+    belong to square ``q = j n + i``; sides ``3q``, ``3q+1``, ``3q+2`` are its
+    bottom, left and diagonal sides, so neighbouring elements have nearby
+    indices.
+    """
+    if n < 1:
+        raise ValueError("n must be >= 1")
+    hx, hy = lx / n, ly / n
+    ii, jj = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    X = x0 + ii * hx
+    Y = y0 + jj * hy
+    if jitter > 0 and n > 1:
+        rng = np.random.default_rng(seed)
+        dx = rng.uniform(-jitter * hx, jitter * hx, size=(n - 1, n - 1))
+        dy = rng.uniform(-jitter * hy, jitter * hy, size=(n - 1, n - 1))
+        X = X.copy(); Y = Y.copy()
+        X[1:n, 1:n] += dx
+        Y[1:n, 1:n] += dy
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="xy")
+    i = i.ravel(); j = j.ravel()            # square q = j*n + i, i fastest
+    q = j * n + i
+    E = 2 * n * n
+    S = 3 * n * n
+    swx, swy = X[i, j], Y[i, j]
+    sex, sey = X[i + 1, j], Y[i + 1, j]
+    nex, ney = X[i + 1, j + 1], Y[i + 1, j + 1]
+    nwx, nwy = X[i, j + 1], Y[i, j + 1]
+    V = np.empty((6, E))
+    V[:, 0::2] = (swx, swy, sex, sey, nex, ney)      # lower (SW, SE, NE)
+    V[:, 1::2] = (swx, swy, nex, ney, nwx, nwy)      # upper (SW, NE, NW)
+    qr = j * n + (i + 1) % n                          # square to the right
+    qu = ((j + 1) % n) * n + i                        # square above
+    ql = j * n + (i - 1) % n                          # square to the left
+    qd = ((j - 1) % n) * n + i                        # square below
+    es = np.empty((3, E), dtype=np.int64)
+    es[:, 0::2] = (3 * q, 3 * qr + 1, 3 * q + 2)
+    es[:, 1::2] = (3 * q + 2, 3 * qu, 3 * q + 1)
+    le = np.empty(S, dtype=np.int64); re = np.empty(S, dtype=np.int64)
+    ls = np.empty(S, dtype=np.int64); rs = np.empty(S, dtype=np.int64)
+    le[0::3], ls[0::3], re[0::3], rs[0::3] = 2 * q, 0, 2 * qd + 1, 1      # bottom
+    le[1::3], ls[1::3], re[1::3], rs[1::3] = 2 * q + 1, 2, 2 * ql, 1      # left
+    le[2::3], ls[2::3], re[2::3], rs[2::3] = 2 * q, 2, 2 * q + 1, 0       # diagonal
+    m = Mesh(*V, *es, le, re, ls, rs,
+             meta=dict(kind="periodic_square", n=n, lx=lx, ly=ly, x0=x0, y0=y0,
+                       jitter=jitter, seed=seed, h=min(hx, hy)))
+    return m
+
+
+def dirichlet_square(n: int, lx: float = 1.0, ly: float = 1.0, x0: float = 0.0,
+                     y0: float = 0.0, jitter: float = 0.0, seed: int = 0,
+                     tag: int = -1) -> Mesh:
+    """Same triangulation as :func:`periodic_square` but with the outer sides
+    as boundary sides tagged ``tag`` (-1 is the advection solver's exact
+    Dirichlet boundary, 2dadvec_kernels.cu:492-517).  Boundary sides are sorted
+    first, as the reference's mesh converter does (genmesh.py:244-284)."""
+    m = periodic_square(n, lx, ly, x0, y0, jitter, seed)
+    i = np.arange(n * n) % n
+    j = np.arange(n * n) // n
+    bottom = 3 * np.arange(n * n)
+    left = bottom + 1
+    re = m.right_elem.astype(np.int64).copy()
+    rs = m.right_side.astype(np.int64).copy()
+    re[bottom[j == 0]] = tag; rs[bottom[j == 0]] = -1
+    re[left[i == 0]] = tag; rs[left[i == 0]] = -1
+    # sides on the top and right boundary are owned (as left element) by the
+    # elements at the top / right; they currently point across the periodic
+    # seam, so rebuild them as boundary sides of the top/right elements.
+    E = m.num_elem
+    es = np.stack([m.elem_s1, m.elem_s2, m.elem_s3], axis=1).astype(np.int64)
+    le = m.left_elem.astype(np.int64).copy()
+    ls = m.left_side.astype(np.int64).copy()
+    V = [a.copy() for a in m.vertices()]
+    extra_le, extra_ls = [], []
+    S0 = m.num_sides
+    # top row upper triangles: local side 1 (NE->NW) was the bottom side of row 0
+    for q in np.nonzero(j == n - 1)[0]:
+        e = 2 * q + 1
+        es[e, 1] = S0 + len(extra_le)
+        extra_le.append(e); extra_ls.append(1)
+    # right column lower triangles: local side 1 (SE->NE) was the left side of column 0
+    for q in np.nonzero(i == n - 1)[0]:
+        e = 2 * q
+        es[e, 1] = S0 + len(extra_le)
+        extra_le.append(e); extra_ls.append(1)
+    le = np.concatenate([le, np.array(extra_le, dtype=np.int64)])
+    ls = np.concatenate([ls, np.array(extra_ls, dtype=np.int64)])
+    re = np.concatenate([re, np.full(len(extra_le), tag, dtype=np.int64)])
+    rs = np.concatenate([rs, np.full(len(extra_le), -1, dtype=np.int64)])
+    # boundary sides first (stable), then interior
+    order = np.concatenate([np.nonzero(re < 0)[0], np.nonzero(re >= 0)[0]])
+    inv = np.empty_like(order); inv[order] = np.arange(order.size)
+    es = inv[es]
+    out = Mesh(*V, es[:, 0], es[:, 1], es[:, 2], le[order], re[order], ls[order], rs[order],
+               meta=dict(m.meta, kind="dirichlet_square", tag=tag))
+    out.check()
+    return out
+
+
+def scramble(m: Mesh, seed: int = 0, rotate: bool = True, swap: bool = True,
+             permute: bool = True) -> Mesh:
+    """Return an equivalent mesh with shuffled element and side numbering,
+    cyclically rotated vertex order and swapped left/right roles, so that
+    every combination of local side numbers occurs (tests only)."""
+    rng = np.random.default_rng(seed)
+    E, S = m.num_elem, m.num_sides
+    V = np.stack(m.vertices()).reshape(6, E)
+    es = np.stack(m.elem_sides(), axis=1).astype(np.int64)
+    le, re = m.left_elem.astype(np.int64).copy(), m.right_elem.astype(np.int64).copy()
+    ls, rs = m.left_side.astype(np.int64).copy(), m.right_side.astype(np.int64).copy()
+    if rotate:
+        r = rng.integers(0, 3, size=E)
+        P = V.reshape(3, 2, E)
+        idx = (np.arange(3)[:, None] + r[None, :]) % 3           # new k <- old (k+r)
+        P = np.take_along_axis(P, idx[:, None, :].repeat(2, axis=1), axis=0)
+        V = P.reshape(6, E)
+        es = np.take_along_axis(es, (np.arange(3)[None, :] + r[:, None]) % 3, axis=1)
+        ls = (ls - r[le]) % 3
+        inter = re >= 0
+        rs[inter] = (rs[inter] - r[re[inter]]) % 3
+    if swap:
+        sw = (rng.random(S) < 0.5) & (re >= 0)
+        le[sw], re[sw] = re[sw].copy(), le[sw].copy()
+        ls[sw], rs[sw] = rs[sw].copy(), ls[sw].copy()
+    if permute:
+        pe = rng.permutation(E)          # new element index of old element
+        ps = rng.permutation(S)          # new side index of old side
+        inv_e = np.empty(E, dtype=np.int64); inv_e[pe] = np.arange(E)
+        inv_s = np.empty(S, dtype=np.int64); inv_s[ps] = np.arange(S)
+        V = V[:, inv_e]
+        es = ps[es[inv_e]]
+        le, ls = pe[le[inv_s]], ls[inv_s]
+        re_old, rs = re[inv_s], rs[inv_s]
+        re = np.where(re_old >= 0, pe[np.maximum(re_old, 0)], re_old)
+    out = Mesh(*V, es[:, 0], es[:, 1], es[:, 2], le, re, ls, rs,
+               meta=dict(m.meta, scrambled=seed))
+    out.check()
+    return out

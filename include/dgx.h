@@ -1,0 +1,170 @@
+/*
+ * dgx.h -- C ABI of the GB300-native 2D discontinuous-Galerkin RHS and time-step
+ * core (a drop-in for thePerv/DGCUDA's 2D DG hot path).
+ *
+ * Plain C: pointers, sizes and status codes only; no CUDA or C++ types.  Streams
+ * are passed as `void *` holding a `cudaStream_t` (NULL = the legacy default
+ * stream).  Every function returns an int status (DGX_OK == 0, negative on
+ * error) and never exits the process; `dgx_status_string` names a status and
+ * `dgx_last_error` gives the message of the last failure on the calling thread.
+ *
+ * Layouts follow the reference:
+ *   mesh    V1x..V3y[num_elem] (FP64, counter-clockwise), elem_s1..3[num_elem],
+ *           left_elem/right_elem/left_side_number/right_side_number[num_sides]
+ *           (src/2d/conservation/conserv.cu:118-192; right_elem < 0 marks a
+ *           boundary side of type -1/-2/-3, conserv_kernels.cu:657-679);
+ *   state   c[n * num_elem * n_p + i * num_elem + e] for variable n, mode i,
+ *           element e (src/2d/conservation/conserv_kernels.cu:21,183), in the
+ *           reference's orthonormal Gram-Schmidt monomial basis (src/2d/basis.cu).
+ *
+ * Handles are not thread-safe: use one host thread per handle.  Device buffers
+ * are owned by the handle.
+ */
+#ifndef DGX_H
+#define DGX_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DGX_VERSION 1
+
+enum dgx_status {
+    DGX_OK = 0,
+    DGX_ERR_INVALID = -1,      /* bad argument or inconsistent mesh            */
+    DGX_ERR_CUDA = -2,         /* a CUDA call failed                           */
+    DGX_ERR_NOMEM = -3,        /* device or host allocation failed             */
+    DGX_ERR_UNSUPPORTED = -4,  /* valid request outside what this build serves */
+    DGX_ERR_NONFINITE = -5,    /* the state holds NaN/Inf or negative density  */
+    DGX_ERR_BUSY = -6,         /* admission refused (budget or queue full)     */
+    DGX_ERR_NOT_FOUND = -7,    /* unknown request id                           */
+    DGX_ERR_TIMEOUT = -8       /* a bounded wait ran out                       */
+};
+
+enum dgx_equation { DGX_ADVECTION = 0, DGX_EULER = 1 };
+enum dgx_flux { DGX_FLUX_CENTRAL = 0, DGX_FLUX_LLF = 1 };
+enum dgx_precision { DGX_FP32 = 0, DGX_FP32_BF16X3 = 1, DGX_FP64 = 2 };
+enum dgx_integrator { DGX_RK4 = 0 };
+enum dgx_dt_mode { DGX_DT_FIXED = 0, DGX_DT_CFL = 1 };
+
+/* Built-in initial conditions (projected with the degree-2p rule, as the
+ * reference's init_conditions, conserv_kernels.cu:167-187).  params[8]:
+ *   GAUSSIAN      u = exp(-((x-x0)^2+(y-y0)^2)/w)        {x0, y0, w, Lx, Ly}
+ *   POLY          u = (x-y)^alpha                         {alpha}
+ *   DENSITY_WAVE  rho = 1 + A sin(2 pi k (x+y)), u, v, p  {A, u, v, p, k}
+ *   VORTEX        isentropic vortex on a free stream      {x0, y0, beta, u, v, Lx, Ly}
+ *   CONSTANT      constant state                          {rho, u, v, p} (advection: {u})
+ * Lx, Ly > 0 take distances to the nearest periodic image. */
+enum dgx_ic {
+    DGX_IC_GAUSSIAN = 0,
+    DGX_IC_POLY = 1,
+    DGX_IC_DENSITY_WAVE = 2,
+    DGX_IC_VORTEX = 3,
+    DGX_IC_CONSTANT = 4
+};
+
+typedef struct dgx_mesh dgx_mesh;
+typedef struct dgx_solver dgx_solver;
+
+typedef struct dgx_solver_desc {
+    int order;       /* p, 0..5 (src/2d/conservation/conserv.cu:61-80)            */
+    int equation;    /* dgx_equation                                                */
+    int flux;        /* dgx_flux: CENTRAL (advection reference), LLF (Euler)        */
+    int precision;   /* dgx_precision                                               */
+    int integrator;  /* dgx_integrator                                              */
+    double gamma;    /* ratio of specific heats (problem file's get_GAMMA)          */
+    double ax, ay;   /* advection velocity (reference: (1,1), 2dadvec_kernels.cu:150-155) */
+} dgx_solver_desc;
+
+/* --- library ---------------------------------------------------------------- */
+int dgx_version(void);
+const char *dgx_status_string(int status);
+const char *dgx_last_error(void);
+
+/* Basis and quadrature tables in FP64 for order p (replaces set_quadrature,
+ * src/2d/conservation/conserv.cu:37-107, and preval_basis, src/2d/basis.cu:150-226).
+ * dims[3] = {n_p, n_quad, n_quad1d}; any output pointer may be NULL.
+ * basis/grad_x/grad_y are [i*n_quad + j] (grad_* premultiplied by the weights),
+ * side is [side*n_p*n_quad1d + i*n_quad1d + j], vertex is [3*i + v]. */
+int dgx_tables(int p, int *dims, double *r1, double *r2, double *w, double *r_oned,
+               double *w_oned, double *basis, double *grad_x, double *grad_y,
+               double *basis_side, double *basis_vertex);
+
+/* --- mesh ------------------------------------------------------------------- */
+/* Upload a mesh and compute its geometric factors in FP64 on the device
+ * (replaces read_mesh + init_gpu + the preval_* kernels,
+ * src/2d/conservation/conserv.cu:118-321, conserv_kernels.cu:338-514).
+ * Host pointers.  The edge normal is oriented out of the left element and the
+ * side length is taken from the left element's local side. */
+int dgx_mesh_create(int num_elem, int num_sides, const double *V1x, const double *V1y,
+                    const double *V2x, const double *V2y, const double *V3x,
+                    const double *V3y, const int *elem_s1, const int *elem_s2,
+                    const int *elem_s3, const int *left_elem, const int *right_elem,
+                    const int *left_side_number, const int *right_side_number,
+                    dgx_mesh **out);
+int dgx_mesh_destroy(dgx_mesh *mesh);
+/* FP64 geometric factors copied to host arrays (NULL to skip): J, x_r, y_r,
+ * x_s, y_s, inscribed diameter per element; length, Nx, Ny per side. */
+int dgx_mesh_geometry(const dgx_mesh *mesh, double *J, double *xr, double *yr, double *xs,
+                      double *ys, double *diameter, double *s_length, double *Nx,
+                      double *Ny);
+int dgx_mesh_min_diameter(const dgx_mesh *mesh, double *out);
+int dgx_mesh_info(const dgx_mesh *mesh, int *num_elem, int *num_sides, int *num_boundary);
+
+/* --- solver ----------------------------------------------------------------- */
+int dgx_solver_create(dgx_mesh *mesh, const dgx_solver_desc *desc, dgx_solver **out);
+int dgx_solver_destroy(dgx_solver *solver);
+/* num_vars (1 or 4), n_p, bytes of one state vector, total device bytes held */
+int dgx_solver_info(const dgx_solver *solver, int *num_vars, int *n_p, size_t *state_bytes,
+                    size_t *device_bytes);
+
+/* State in the reference layout, host FP64 (any precision) or host FP32. */
+int dgx_set_state(dgx_solver *solver, const double *c);
+int dgx_get_state(dgx_solver *solver, double *c);
+int dgx_set_state_f32(dgx_solver *solver, const float *c, void *stream);
+int dgx_get_state_f32(dgx_solver *solver, float *c, void *stream);
+/* Device pointer of the resident state (FP32, or FP64 in DGX_FP64 precision). */
+int dgx_state_device_ptr(dgx_solver *solver, void **ptr);
+/* L2-project a built-in initial condition onto the state (FP64 on the device). */
+int dgx_project_ic(dgx_solver *solver, int ic, const double *params);
+
+/* One RHS evaluation on device buffers in the solver's precision:
+ * k = dt / J * (volume + sum of the three lifted edge fluxes), the contract of
+ * eval_surface + eval_volume + eval_rhs (src/2d/conservation/time_integrator.cu:
+ * 130-188, conserv_kernels.cu:697-811).  u and k must not alias. */
+int dgx_rhs_eval(dgx_solver *solver, const void *u, void *k, double dt, double t,
+                 void *stream);
+
+/* Time step size: FIXED uses dt; CFL uses dt = cfl * min diameter / max wave
+ * speed / (2p+1) from cell averages (time_integrator.cu:252-270,
+ * euler.cu:252-278), computed and kept on the device. */
+int dgx_set_dt(dgx_solver *solver, int dt_mode, double dt, double cfl);
+/* End time: the last step is clipped to land on it (time_integrator.cu:263-270);
+ * t_end <= 0 disables clipping. */
+int dgx_set_end_time(dgx_solver *solver, double t_end);
+/* One RK stage s = 0..3 of the classic RK4 on the resident state
+ * (rk_tempstorage / rk4, time_integrator.cu:194-218); stage 0 also fixes dt. */
+int dgx_rk_stage(dgx_solver *solver, int stage, void *stream);
+/* One full time step (CFL + four stages), asynchronous on `stream`. */
+int dgx_step(dgx_solver *solver, void *stream);
+/* Advance until t_end or max_steps steps (time_integrate_rk4,
+ * time_integrator.cu:221-434); synchronous. */
+int dgx_run(dgx_solver *solver, double t_end, int max_steps, int *steps, double *t,
+            void *stream);
+/* Current simulation time and last dt (synchronises the stream). */
+int dgx_time(dgx_solver *solver, double *t, double *dt, void *stream);
+int dgx_reset_time(dgx_solver *solver, double t);
+/* Conserved totals  int u_n dx  in FP64 (deterministic device reduction). */
+int dgx_conserved_totals(dgx_solver *solver, double *out, void *stream);
+/* Maximum cell-average wave speed of the resident state. */
+int dgx_max_wave_speed(dgx_solver *solver, double *out, void *stream);
+/* Number of CUDA kernels this solver has launched so far. */
+int dgx_launch_count(const dgx_solver *solver, long long *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DGX_H */

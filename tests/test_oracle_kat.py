@@ -1,0 +1,127 @@
+"""Known-answer tests of the FP64 oracle (CPU): basis orthonormality,
+quadrature exactness, free-stream preservation, discrete conservation,
+linearity, and invariance under renumbering of the mesh (the reference's own
+test ideas, src/2d/test_all.cu:83-707, on periodic meshes)."""
+import math
+
+import numpy as np
+import pytest
+
+from dgcuda_gb300.mesh import periodic_square, scramble
+
+
+@pytest.mark.parametrize("p", range(6))
+def test_basis_orthonormal_and_rule_exact(p, oracle_mod):
+    T = oracle_mod.tables(p)
+    M = (T["phi"] * T["w"]) @ T["phi"].T
+    np.testing.assert_allclose(M, np.eye(T["np"]), atol=1e-13)
+    for a in range(2 * p + 1):
+        for b in range(2 * p + 1 - a):
+            exact = math.factorial(a) * math.factorial(b) / math.factorial(a + b + 2)
+            got = np.sum(T["w"] * T["r1"] ** a * T["r2"] ** b)
+            assert abs(got - exact) < 1e-14, (a, b)
+    for d in range(2 * p + 2):
+        exact = (1 - (-1) ** (d + 1)) / (d + 1)
+        assert abs(np.sum(T["w1"] * T["s1"] ** d) - exact) < 1e-14
+    assert abs(T["phi"][0, 0] - math.sqrt(2)) < 1e-14
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_free_stream_preserved(p, oracle_mod):
+    orc = oracle_mod
+    m = scramble(periodic_square(5, jitter=0.2, seed=p), seed=p)
+    o = orc.Oracle(m, p, orc.EULER, orc.LLF)
+    c = o.project(orc.IC_CONSTANT, (1.3, 0.4, -0.7, 2.0))
+    k = o.rhs(c, 1.0)
+    assert np.abs(k).max() < 1e-11 * np.abs(c).max()
+    oa = orc.Oracle(m, p, orc.ADVECTION, orc.LLF, a=(0.3, -1.1))
+    ca = oa.project(orc.IC_CONSTANT, (2.5,))
+    assert np.abs(oa.rhs(ca)).max() < 1e-10
+
+
+@pytest.mark.parametrize("eq", ["euler", "advection"])
+def test_rhs_conserves_totals(eq, oracle_mod):
+    orc = oracle_mod
+    m = scramble(periodic_square(6, jitter=0.2, seed=3), seed=7)
+    if eq == "euler":
+        o = orc.Oracle(m, 3, orc.EULER, orc.LLF)
+        c = o.project(orc.IC_VORTEX, (0.5, 0.5, 2.0, 1.0, 0.3, 1.0, 1.0))
+    else:
+        o = orc.Oracle(m, 3, orc.ADVECTION, orc.LLF, a=(1.0, 0.5))
+        c = o.project(orc.IC_GAUSSIAN, (0.3, 0.6, 0.02, 1.0, 1.0))
+    k = o.rhs(c, 1.0)
+    J = o.geometry()["J"]
+    for n in range(o.nv):
+        # d/dt int u = sum_e J_e/sqrt(2) k_{n,0,e}/dt * J_e... k carries 1/J
+        rate = np.sum(k[n, 0] * J)
+        scale = np.sum(np.abs(k[n, 0] * J)) + 1e-300
+        assert abs(rate) < 1e-12 * scale
+
+
+def test_advection_rhs_linear(oracle_mod):
+    orc = oracle_mod
+    m = periodic_square(5, jitter=0.1, seed=1)
+    rng = np.random.default_rng(0)
+    for flux in (orc.CENTRAL, orc.LLF):
+        o = orc.Oracle(m, 2, orc.ADVECTION, flux, a=(1.0, 1.0))
+        u, v = rng.standard_normal(o.shape), rng.standard_normal(o.shape)
+        lhs = o.rhs(2.0 * u - 3.0 * v)
+        np.testing.assert_allclose(lhs, 2.0 * o.rhs(u) - 3.0 * o.rhs(v), atol=1e-11)
+
+
+def test_renumbering_invariance(oracle_mod):
+    """Swapping left/right roles and permuting elements and sides leaves the
+    RHS unchanged up to the permutation; rotating the local vertex order
+    leaves the RHS unchanged as a function (compared at the vertices)."""
+    orc = oracle_mod
+    base = periodic_square(4, lx=10, ly=10, jitter=0.15, seed=5)
+    params = (5.0, 5.0, 3.0, 1.0, 0.5, 10.0, 10.0)
+    o0 = orc.Oracle(base, 3, orc.EULER, orc.LLF)
+    k0 = o0.rhs(o0.project(orc.IC_VORTEX, params))
+    m1 = scramble(base, seed=9, rotate=False)
+    o1 = orc.Oracle(m1, 3, orc.EULER, orc.LLF)
+    k1 = o1.rhs(o1.project(orc.IC_VORTEX, params))
+    # match elements by centroid
+    cx0, cy0 = base.centroids()
+    cx1, cy1 = m1.centroids()
+    i0 = np.lexsort((np.round(cy0, 9), np.round(cx0, 9)))
+    i1 = np.lexsort((np.round(cy1, 9), np.round(cx1, 9)))
+    np.testing.assert_allclose(k1[:, :, i1], k0[:, :, i0], rtol=1e-12, atol=1e-12)
+    m2 = scramble(base, seed=11, rotate=True, swap=True, permute=False)
+    o2 = orc.Oracle(m2, 3, orc.EULER, orc.LLF)
+    k2 = o2.rhs(o2.project(orc.IC_VORTEX, params))
+    T = orc.tables(3)
+    vals0 = np.einsum("nie,iv->nev", k0, T["vert"])   # RHS at V1, V2, V3
+    vals2 = np.einsum("nie,iv->nev", k2, T["vert"])
+    # vertex v of the rotated element is vertex (v + r) of the original one
+    for e in range(base.num_elem):
+        r = [rr for rr in range(3)
+             if np.isclose(m2.V1x[e], base.vertices()[2 * rr][e]) and np.isclose(m2.V1y[e], base.vertices()[2 * rr + 1][e])][0]
+        np.testing.assert_allclose(vals2[:, e, :], np.roll(vals0[:, e, :], -r, axis=1), rtol=1e-9, atol=1e-9)
+
+
+def test_cfl_rule(oracle_mod):
+    orc = oracle_mod
+    m = periodic_square(4, jitter=0.15, seed=2)
+    o = orc.Oracle(m, 2, orc.EULER, orc.LLF)
+    c = o.project(orc.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
+    dt = o.cfl_dt(c, 0.7)
+    assert abs(dt - 0.7 * o.min_diameter() / o.max_lambda(c) / 5.0) < 1e-15
+    c1, n, t = o.run(c, t_end=10 * dt + 0.5 * dt)
+    assert n == 11 and abs(t - 10.5 * dt) < 1e-12
+
+
+def test_advection_convergence(oracle_mod):
+    """Smooth advection converges at order ~p+1 (LLF flux)."""
+    orc = oracle_mod
+    errs = []
+    for n in (8, 16):
+        m = periodic_square(n, jitter=0.1, seed=n)
+        o = orc.Oracle(m, 2, orc.ADVECTION, orc.LLF, a=(1.0, 1.0))
+        params = (0.5, 0.5, 0.02, 1.0, 1.0)
+        c = o.project(orc.IC_GAUSSIAN, params)
+        c1, _, t = o.run(c, t_end=0.25, dt=0.02 / n)
+        exact = o.project(orc.IC_GAUSSIAN, (0.75, 0.75, 0.02, 1.0, 1.0))
+        errs.append(np.linalg.norm(c1 - exact) / np.linalg.norm(exact))
+    rate = math.log2(errs[0] / errs[1])
+    assert rate > 2.3, errs
