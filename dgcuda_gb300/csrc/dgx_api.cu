@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 #include <new>
 #include <vector>
@@ -47,7 +48,7 @@ int dalloc(T **p, size_t count, size_t *acct) {
 void mesh_free(dgx_mesh *m) {
     MeshDev &d = m->d;
     void *ptrs[] = {d.V, d.elem_s, d.sides, d.J, d.xr, d.yr, d.xs, d.ys, d.diam, d.len, d.nx,
-                    d.ny, d.nbr, d.geo32, d.fn32, d.geo64, d.fn64};
+                    d.ny, d.nbr, d.halo_off, d.halo_list, d.geo32, d.fn32, d.geo64, d.fn64};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete m;
@@ -58,6 +59,42 @@ void mesh_release(dgx_mesh *m) {
 }
 
 cudaStream_t as_stream(void *s) { return static_cast<cudaStream_t>(s); }
+
+// Tiles of kTile consecutive elements: for every element side, the shared-memory
+// slot that will hold the neighbour's trace (inside the tile: 3*l + side; outside:
+// the tile's next halo slot), and per tile the list of halo (element, side) pairs.
+void build_tiles(int E, const int *const es[3], const int *le, const int *re, const int *ls,
+                 const int *rs, std::vector<int> &words, std::vector<int> &hoff,
+                 std::vector<int> &hlist, int &max_halo) {
+    const int ntiles = (E + kTile - 1) / kTile;
+    words.assign(3 * static_cast<size_t>(E), 0);
+    hoff.assign(ntiles + 1, 0);
+    hlist.clear();
+    hlist.reserve(E);
+    max_halo = 0;
+    for (int b = 0; b < ntiles; ++b) {
+        hoff[b] = static_cast<int>(hlist.size());
+        const int lo = b * kTile, hi = std::min(E, lo + kTile);
+        for (int e = lo; e < hi; ++e)
+            for (int k = 0; k < 3; ++k) {
+                const int s = es[k][e];
+                const int il = (le[s] == e) ? 1 : 0;   // the reference's rule (time_integrator.cu:153)
+                const int ne = il ? re[s] : le[s];
+                const int ns = il ? rs[s] : ls[s];
+                int w;
+                if (ne < 0) w = ne;
+                else if (ne >= lo && ne < hi) w = pack_side_word(3 * (ne - lo) + ns, il);
+                else {
+                    const int h = static_cast<int>(hlist.size()) - hoff[b];
+                    hlist.push_back(pack_halo(ne, ns));
+                    w = pack_side_word(3 * kTile + h, il);
+                }
+                words[static_cast<size_t>(k) * E + e] = w;
+            }
+        max_halo = std::max(max_halo, static_cast<int>(hlist.size()) - hoff[b]);
+    }
+    hoff[ntiles] = static_cast<int>(hlist.size());
+}
 
 size_t elem_size(const SolverDev &s) { return s.precision == DGX_FP64 ? sizeof(double) : sizeof(float); }
 
@@ -77,6 +114,9 @@ int stage_launch(dgx_solver *sv, int mode, const void *u, const void *c, void *a
     a.acc = acc;
     a.out = out;
     a.nbr = m.nbr;
+    a.halo_off = m.halo_off;
+    a.halo_list = m.halo_list;
+    a.nslot = 3 * kTile + m.max_halo;
     a.scal = s.scal;
     a.dt = dt;
     a.t = t;
@@ -224,7 +264,14 @@ int dgx_mesh_create(int num_elem, int num_sides, const double *V1x, const double
     rc |= dalloc(&d.J, E, &acct); rc |= dalloc(&d.xr, E, &acct); rc |= dalloc(&d.yr, E, &acct);
     rc |= dalloc(&d.xs, E, &acct); rc |= dalloc(&d.ys, E, &acct); rc |= dalloc(&d.diam, E, &acct);
     rc |= dalloc(&d.len, S, &acct); rc |= dalloc(&d.nx, S, &acct); rc |= dalloc(&d.ny, S, &acct);
+    std::vector<int> words, hoff, hlist;
+    build_tiles(num_elem, es, left_elem, right_elem, left_side_number, right_side_number, words,
+                hoff, hlist, d.max_halo);
+    d.num_tiles = static_cast<int>(hoff.size()) - 1;
+    d.total_halo = static_cast<int>(hlist.size());
     rc |= dalloc(&d.nbr, 3 * E, &acct);
+    rc |= dalloc(&d.halo_off, hoff.size(), &acct);
+    rc |= dalloc(&d.halo_list, hlist.size(), &acct);
     rc |= dalloc(&d.geo32, 5 * E, &acct); rc |= dalloc(&d.fn32, 9 * E, &acct);
     rc |= dalloc(&d.geo64, 5 * E, &acct); rc |= dalloc(&d.fn64, 9 * E, &acct);
     if (rc) { mesh_free(m); return DGX_ERR_NOMEM; }
@@ -235,6 +282,10 @@ int dgx_mesh_create(int num_elem, int num_sides, const double *V1x, const double
         ce = cudaMemcpy(d.elem_s + i * E, es[i], E * sizeof(int), cudaMemcpyHostToDevice);
     for (int i = 0; i < 4 && ce == cudaSuccess; ++i)
         ce = cudaMemcpy(d.sides + i * S, sd[i], S * sizeof(int), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(d.nbr, words.data(), words.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(d.halo_off, hoff.data(), hoff.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess && !hlist.empty())
+        ce = cudaMemcpy(d.halo_list, hlist.data(), hlist.size() * sizeof(int), cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) { set_error("mesh upload failed: %s", cudaGetErrorString(ce)); mesh_free(m); return DGX_ERR_CUDA; }
     rc = mesh_geometry(d, nullptr);
     if (!rc && cudaDeviceSynchronize() != cudaSuccess) { set_error("geometry kernels failed"); rc = DGX_ERR_CUDA; }

@@ -40,10 +40,17 @@ enum StatusBits : unsigned int {
     kStatusNegative = 2u,    // non-positive density or pressure in a cell average
 };
 
-// Element-side connectivity word: neighbour element e >= 0 packed as
-// e*8 + is_left*4 + neighbour's local side; a boundary side stores its
-// (negative) boundary tag.
-DGX_HD inline int pack_nbr(int e, int is_left, int side) { return e * 8 + is_left * 4 + side; }
+// Elements are processed in tiles of kTile consecutive elements, one CTA per
+// tile.  The side traces a tile needs live in shared memory in "slots": slot
+// 3*l + k holds the trace of the tile's element l on its local side k, slots
+// 3*kTile + h hold the tile's halo (traces of neighbours outside the tile).
+constexpr int kTile = 128;
+
+// Element-side word: (slot of the neighbour's trace) * 2 + is_left, or the
+// (negative) boundary tag of a boundary side.
+DGX_HD inline int pack_side_word(int slot, int is_left) { return slot * 2 + is_left; }
+// Halo entry: neighbour element * 4 + neighbour's local side.
+DGX_HD inline int pack_halo(int e, int side) { return e * 4 + side; }
 
 // Mesh geometry, computed in FP64 on the device at creation.
 struct MeshDev {
@@ -57,7 +64,10 @@ struct MeshDev {
     double *len = nullptr, *nx = nullptr, *ny = nullptr;   // [S]
     double min_diam = 0.0;
     // per-element hot-path arrays
-    int *nbr = nullptr;         // [3][E] packed neighbour words
+    int *nbr = nullptr;         // [3][E] element-side words (pack_side_word)
+    int *halo_off = nullptr;    // [num_tiles + 1] CSR offsets into halo_list
+    int *halo_list = nullptr;   // [total halo] pack_halo entries, per tile
+    int num_tiles = 0, max_halo = 0, total_halo = 0;
     float *geo32 = nullptr;     // [5][E] 1/J, x_r, y_r, x_s, y_s
     float *fn32 = nullptr;      // [3 sides][3][E] nx, ny, len/2 (normal out of the side's left element)
     double *geo64 = nullptr;    // same in FP64
@@ -119,6 +129,9 @@ struct StageArgs {
     void *acc;         // accumulator
     void *out;         // k (mode 0), next stage input (1..3), state (4)
     const int *nbr;
+    const int *halo_off;
+    const int *halo_list;
+    int nslot;         // 3*kTile + max halo of the mesh
     const void *geo;
     const void *fn;
     const double *scal;   // device dt/t (modes 1..4); may be null for mode 0

@@ -79,21 +79,14 @@ __global__ void side_geometry_kernel(MeshDev m) {
     m.len[s] = len; m.nx[s] = nx; m.ny[s] = ny;
 }
 
-// element-side connectivity and side factors for the hot path
+// side factors for the hot path, per element and local side
 __global__ void elem_side_kernel(MeshDev m) {
     const int E = m.num_elem;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
-    const size_t SE = E, SS = m.num_sides;
+    const size_t SE = E;
     for (int k = 0; k < 3; ++k) {
         const int s = m.elem_s[k * SE + e];
-        const int le = m.sides[s], re = m.sides[SS + s];
-        const int lsn = m.sides[2 * SS + s], rsn = m.sides[3 * SS + s];
-        const int il = (le == e) ? 1 : 0;   // the reference's rule (time_integrator.cu:153)
-        int word;
-        if (re < 0) word = re;
-        else word = il ? pack_nbr(re, 1, rsn) : pack_nbr(le, 0, lsn);
-        m.nbr[k * SE + e] = word;
         m.fn32[(3 * k + 0) * SE + e] = static_cast<float>(m.nx[s]);
         m.fn32[(3 * k + 1) * SE + e] = static_cast<float>(m.ny[s]);
         m.fn32[(3 * k + 2) * SE + e] = static_cast<float>(0.5 * m.len[s]);

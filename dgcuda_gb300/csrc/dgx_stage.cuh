@@ -4,7 +4,12 @@
 // the arithmetic type.  Each translation unit owns its copy of the constant
 // tables (uploaded by upload_tables_f32/_f64).
 //
-// Per element e the kernel computes, in registers,
+// One CTA per tile of kTile consecutive elements, one thread per element.
+// Phase 1 writes each element's traces on its three sides (p+1 Gauss points)
+// to shared memory and, one halo entry per thread, the traces of the tile's
+// neighbours outside the tile (their gathers issued together); phase 2, after
+// one barrier, reads both traces of every side from shared memory.
+// Per element e the kernel computes
 //   volume   V_i = sum_q gx_iq (Fx ys - Fy xs) + gy_iq (Fy xr - Fx yr)      at U(q)
 //            (src/2d/conservation/conserv_kernels.cu:766-811)
 //   surface  for each local side k: own trace and neighbour trace at the p+1
@@ -27,8 +32,6 @@
 #endif
 
 namespace dgx {
-
-constexpr int kStageThreads = 128;
 
 static __constant__ DGX_REAL c_tab[kTableTotal];
 
@@ -101,78 +104,69 @@ __device__ __forceinline__ void num_flux(const R *UL, const R *UR, R nx, R ny, i
     }
 }
 
+// Shared memory of one CTA: the side tables (for traces on a runtime side) and
+// the trace slots, stored value-major: s_tr[(j*NV + n) * nslot + slot], so that
+// threads reading their own slots 3*tid + k hit distinct banks.
+template <int P, int NV>
+DGX_HD constexpr int side_table_words() { return (3 * num_modes(P) * num_quad1(P) + 3) & ~3; }
+
+template <int P, int NV>
+DGX_HD constexpr size_t stage_smem_bytes(int nslot) {
+    return sizeof(R) * (static_cast<size_t>(side_table_words<P, NV>()) +
+                        static_cast<size_t>(NV) * num_quad1(P) * nslot);
+}
+
 template <int P, int EQ>
-__global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageArgs a) {
+__global__ void __launch_bounds__(kTile, (P <= 3 ? 4 : 2)) stage_kernel(const StageArgs a) {
     using L = Lay<P>;
     constexpr int NP = L::NP, NQ = L::NQ, NQ1 = L::NQ1;
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
-    __shared__ R s_side[3 * NP * NQ1];
-    for (int t = threadIdx.x; t < 3 * NP * NQ1; t += blockDim.x) s_side[t] = c_tab[L::SIDE + t];
-    __syncthreads();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *s_side = reinterpret_cast<R *>(smem_raw);
+    R *s_tr = s_side + side_table_words<P, NV>();
+    const int nslot = a.nslot;
 
-    const int E = a.E;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= E) return;
     R dt;
     if (a.mode == 0) {
         dt = R(a.dt);
     } else {
         dt = R(a.scal[0]);
-        if (dt == R(0)) return;   // the run has reached its end time
+        if (dt == R(0)) return;   // the run has reached its end time (uniform over the grid)
     }
+    const int E = a.E;
+    const int tid = threadIdx.x;
+    const int tile = blockIdx.x;
+    const int e = tile * kTile + tid;
+    const bool live = e < E;
     const size_t SE = static_cast<size_t>(E);
     const R g = R(a.gamma), ax = R(a.ax), ay = R(a.ay);
     const int llf = a.flux == DGX_FLUX_LLF;
     const R *__restrict__ u = static_cast<const R *>(a.u);
 
+    for (int t = tid; t < 3 * NP * NQ1; t += kTile) s_side[t] = c_tab[L::SIDE + t];
+
+    // own coefficients (coalesced: 32 consecutive elements per warp and (n,i))
     R c[NV][NP];
 #pragma unroll
     for (int n = 0; n < NV; ++n)
 #pragma unroll
-        for (int i = 0; i < NP; ++i) c[n][i] = __ldg(u + (n * NP + i) * SE + e);
+        for (int i = 0; i < NP; ++i) c[n][i] = live ? __ldg(u + (n * NP + i) * SE + e) : R(0);
 
-    const R *__restrict__ geo = static_cast<const R *>(a.geo);
-    const R invJ = __ldg(geo + e), xr = __ldg(geo + SE + e), yr = __ldg(geo + 2 * SE + e);
-    const R xs = __ldg(geo + 3 * SE + e), ys = __ldg(geo + 4 * SE + e);
-
-    R rhs[NV][NP];
+    // first halo entry of this thread: issue its gathers before any compute
+    const int h0 = __ldg(a.halo_off + tile), H = __ldg(a.halo_off + tile + 1) - h0;
+    R cn[NV][NP];
+    int hw = tid < H ? __ldg(a.halo_list + h0 + tid) : -1;
+    if (hw >= 0) {
+        const int ne = hw >> 2;
 #pragma unroll
-    for (int n = 0; n < NV; ++n)
+        for (int n = 0; n < NV; ++n)
 #pragma unroll
-        for (int i = 0; i < NP; ++i) rhs[n][i] = R(0);
-
-    // ---- volume integral ------------------------------------------------------
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        R U[NV], fx[NV], fy[NV];
-#pragma unroll
-        for (int n = 0; n < NV; ++n) {
-            R s = R(0);
-#pragma unroll
-            for (int i = 0; i < NP; ++i) s = fma(c[n][i], c_tab[L::PHI + i * NQ + q], s);
-            U[n] = s;
-        }
-        phys_flux<EQ>(U, g, ax, ay, fx, fy);
-#pragma unroll
-        for (int n = 0; n < NV; ++n) {
-            const R hr = fx[n] * ys - fy[n] * xs;
-            const R hs = fy[n] * xr - fx[n] * yr;
-#pragma unroll
-            for (int i = 0; i < NP; ++i)
-                rhs[n][i] = fma(c_tab[L::GX + i * NQ + q], hr, fma(c_tab[L::GY + i * NQ + q], hs, rhs[n][i]));
-        }
+            for (int i = 0; i < NP; ++i) cn[n][i] = __ldg(u + (n * NP + i) * SE + ne);
     }
 
-    // ---- the three sides ----------------------------------------------------
-    const int *__restrict__ nbr = a.nbr;
-    const R *__restrict__ fn = static_cast<const R *>(a.fn);
+    // own traces on the three sides (compile-time side tables)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const int nb = __ldg(nbr + k * SE + e);
-        const R nx = __ldg(fn + (3 * k + 0) * SE + e);
-        const R ny = __ldg(fn + (3 * k + 1) * SE + e);
-        const R hl = __ldg(fn + (3 * k + 2) * SE + e);
-        R UO[NQ1][NV], UN[NQ1][NV];
+    for (int k = 0; k < 3; ++k)
 #pragma unroll
         for (int j = 0; j < NQ1; ++j)
 #pragma unroll
@@ -180,42 +174,93 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageArgs a)
                 R s = R(0);
 #pragma unroll
                 for (int i = 0; i < NP; ++i) s = fma(c[n][i], c_tab[L::SIDE + (k * NP + i) * NQ1 + j], s);
-                UO[j][n] = s;
+                s_tr[(j * NV + n) * nslot + 3 * tid + k] = s;
             }
-        int il = 1;
-        if (nb >= 0) {
-            const int ne = nb >> 3, ns = nb & 3;
-            il = (nb >> 2) & 1;
-            R cn[NV][NP];
+    __syncthreads();   // s_side ready
+
+    // halo traces: the tile's neighbours outside the tile, on their own side
+    // and in their own point order (a runtime side: tables from shared memory)
+    for (int h = tid; h < H; h += kTile) {
+        if (h != tid) {
+            hw = __ldg(a.halo_list + h0 + h);
+            const int ne = hw >> 2;
 #pragma unroll
             for (int n = 0; n < NV; ++n)
 #pragma unroll
                 for (int i = 0; i < NP; ++i) cn[n][i] = __ldg(u + (n * NP + i) * SE + ne);
-            const R *ts = s_side + ns * NP * NQ1;
-#pragma unroll
-            for (int j = 0; j < NQ1; ++j)
-#pragma unroll
-                for (int n = 0; n < NV; ++n) {
-                    R s = R(0);
-#pragma unroll
-                    for (int i = 0; i < NP; ++i) s = fma(cn[n][i], ts[i * NQ1 + (NQ1 - 1 - j)], s);
-                    UN[j][n] = s;
-                }
-        } else {
-            // boundary sides are rejected at solver creation; mirror state
-#pragma unroll
-            for (int j = 0; j < NQ1; ++j)
-#pragma unroll
-                for (int n = 0; n < NV; ++n) UN[j][n] = UO[j][n];
         }
+        const R *ts = s_side + (hw & 3) * NP * NQ1;
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j)
+#pragma unroll
+            for (int n = 0; n < NV; ++n) {
+                R s = R(0);
+#pragma unroll
+                for (int i = 0; i < NP; ++i) s = fma(cn[n][i], ts[i * NQ1 + j], s);
+                s_tr[(j * NV + n) * nslot + 3 * kTile + h] = s;
+            }
+    }
+
+    R rhs[NV][NP];
+#pragma unroll
+    for (int n = 0; n < NV; ++n)
+#pragma unroll
+        for (int i = 0; i < NP; ++i) rhs[n][i] = R(0);
+
+    R invJ = R(0);
+    if (live) {
+        const R *__restrict__ geo = static_cast<const R *>(a.geo);
+        invJ = __ldg(geo + e);
+        const R xr = __ldg(geo + SE + e), yr = __ldg(geo + 2 * SE + e);
+        const R xs = __ldg(geo + 3 * SE + e), ys = __ldg(geo + 4 * SE + e);
+        // ---- volume integral ----------------------------------------------------
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            R U[NV], fx[NV], fy[NV];
+#pragma unroll
+            for (int n = 0; n < NV; ++n) {
+                R s = R(0);
+#pragma unroll
+                for (int i = 0; i < NP; ++i) s = fma(c[n][i], c_tab[L::PHI + i * NQ + q], s);
+                U[n] = s;
+            }
+            phys_flux<EQ>(U, g, ax, ay, fx, fy);
+#pragma unroll
+            for (int n = 0; n < NV; ++n) {
+                const R hr = fx[n] * ys - fy[n] * xs;
+                const R hs = fy[n] * xr - fx[n] * yr;
+#pragma unroll
+                for (int i = 0; i < NP; ++i)
+                    rhs[n][i] = fma(c_tab[L::GX + i * NQ + q], hr, fma(c_tab[L::GY + i * NQ + q], hs, rhs[n][i]));
+            }
+        }
+    }
+    __syncthreads();   // all traces of the tile and its halo are in shared memory
+    if (!live) return;
+
+    // ---- the three sides --------------------------------------------------------
+    const int *__restrict__ nbr = a.nbr;
+    const R *__restrict__ fn = static_cast<const R *>(a.fn);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int word = __ldg(nbr + k * SE + e);
+        const R nx = __ldg(fn + (3 * k + 0) * SE + e);
+        const R ny = __ldg(fn + (3 * k + 1) * SE + e);
+        const R hl = __ldg(fn + (3 * k + 2) * SE + e);
+        const int own = 3 * tid + k;
+        // a boundary side (rejected at solver creation) would mirror the own trace
+        const int slot = word >= 0 ? (word >> 1) : own;
+        const int il = word >= 0 ? (word & 1) : 1;
         R Fh[NQ1][NV];
 #pragma unroll
         for (int j = 0; j < NQ1; ++j) {
-            R UL[NV], UR[NV];
+            R UO[NV], UN[NV], UL[NV], UR[NV];
 #pragma unroll
             for (int n = 0; n < NV; ++n) {
-                UL[n] = il ? UO[j][n] : UN[j][n];
-                UR[n] = il ? UN[j][n] : UO[j][n];
+                UO[n] = s_tr[(j * NV + n) * nslot + own];
+                UN[n] = s_tr[((NQ1 - 1 - j) * NV + n) * nslot + slot];
+                UL[n] = il ? UO[n] : UN[n];
+                UR[n] = il ? UN[n] : UO[n];
             }
             num_flux<EQ>(UL, UR, nx, ny, llf, g, ax, ay, Fh[j]);
         }
@@ -286,8 +331,16 @@ __global__ void __launch_bounds__(kStageThreads) stage_kernel(const StageArgs a)
 
 template <int P, int EQ>
 static int launch_one(const StageArgs &a, cudaStream_t st) {
-    const int grid = (a.E + kStageThreads - 1) / kStageThreads;
-    if (grid > 0) stage_kernel<P, EQ><<<grid, kStageThreads, 0, st>>>(a);
+    constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
+    const size_t smem = stage_smem_bytes<P, NV>(a.nslot);
+    static size_t configured = 0;   // dynamic shared memory opted in so far
+    if (smem > 48 * 1024 && smem > configured) {
+        DGX_TRY_CUDA(cudaFuncSetAttribute(stage_kernel<P, EQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          static_cast<int>(smem)));
+        configured = smem;
+    }
+    const int grid = (a.E + kTile - 1) / kTile;
+    if (grid > 0) stage_kernel<P, EQ><<<grid, kTile, smem, st>>>(a);
     DGX_CHECK_LAUNCH();
     return DGX_OK;
 }
