@@ -66,6 +66,7 @@ SIGNATURES = {
     "dgx_time": (None, [_vp, _dp, _dp, _vp]),
     "dgx_reset_time": (None, [_vp, _d]),
     "dgx_conserved_totals": (None, [_vp, _dp, _vp]),
+    "dgx_conserved_totals_static": (None, [_vp, _vp, _vp, _vp]),
     "dgx_max_wave_speed": (None, [_vp, _dp, _vp]),
     "dgx_launch_count": (None, [_vp, C.POINTER(C.c_longlong)]),
 }
