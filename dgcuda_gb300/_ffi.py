@@ -21,6 +21,7 @@ FLUX_CENTRAL, FLUX_LLF = 0, 1
 FP32, FP32_BF16X3, FP64 = 0, 1, 2
 RK4 = 0
 DT_FIXED, DT_CFL = 0, 1
+OPT_PREFETCH = 1
 IC_GAUSSIAN, IC_POLY, IC_DENSITY_WAVE, IC_VORTEX, IC_CONSTANT = 0, 1, 2, 3, 4
 
 
@@ -69,6 +70,15 @@ SIGNATURES = {
     "dgx_conserved_totals_static": (None, [_vp, _vp, _vp, _vp]),
     "dgx_max_wave_speed": (None, [_vp, _dp, _vp]),
     "dgx_launch_count": (None, [_vp, C.POINTER(C.c_longlong)]),
+    "dgx_solver_set_option": (None, [_vp, _i, _i]),
+    "dgx_batch_create": (None, [C.POINTER(_vp), _i, C.POINTER(_vp)]),
+    "dgx_batch_destroy": (None, [_vp]),
+    "dgx_batch_step": (None, [_vp, _vp]),
+    "dgx_batch_run": (None, [_vp, _i, _vp]),
+    "dgx_batch_autotune": (None, [_vp, _i, _vp]),
+    "dgx_batch_info": (None, [_vp, _ip, _ip, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "dgx_batch_class_options": (None, [_vp, _i, _ip, _ip, _ip, _ip]),
+    "dgx_batch_launch_count": (None, [_vp, C.POINTER(C.c_longlong)]),
 }
 
 _lib = None

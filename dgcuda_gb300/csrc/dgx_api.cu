@@ -100,36 +100,9 @@ size_t elem_size(const SolverDev &s) { return s.precision == DGX_FP64 ? sizeof(d
 
 int stage_launch(dgx_solver *sv, int mode, const void *u, const void *c, void *acc, void *out,
                  double dt, double t, cudaStream_t st) {
-    SolverDev &s = sv->s;
-    const MeshDev &m = sv->mesh->d;
-    StageArgs a;
-    a.E = m.num_elem;
-    a.mode = mode;
-    a.flux = s.flux;
-    a.gamma = s.gamma;
-    a.ax = s.ax;
-    a.ay = s.ay;
-    a.u = u;
-    a.c = c;
-    a.acc = acc;
-    a.out = out;
-    a.nbr = m.nbr;
-    a.halo_off = m.halo_off;
-    a.halo_list = m.halo_list;
-    a.nslot = 3 * kTile + m.max_halo;
-    a.scal = s.scal;
-    a.dt = dt;
-    a.t = t;
-    int rc;
-    if (s.precision == DGX_FP64) {
-        a.geo = m.geo64;
-        a.fn = m.fn64;
-        rc = launch_stage_f64(s.order, s.equation, a, st);
-    } else {
-        a.geo = m.geo32;
-        a.fn = m.fn32;
-        rc = launch_stage_f32(s.order, s.equation, a, st);
-    }
+    const StageArgs a = make_stage_args(sv, mode, u, c, acc, out, dt, t);
+    const int rc = sv->s.precision == DGX_FP64 ? launch_stage_f64(sv->s.order, sv->s.equation, a, st)
+                                               : launch_stage_f32(sv->s.order, sv->s.equation, a, st);
     if (!rc) sv->launches++;
     return rc;
 }
@@ -156,6 +129,45 @@ int write_scalar(SolverDev &s, int idx, double v) {
 }
 
 }  // namespace
+
+StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c, void *acc,
+                          void *out, double dt, double t) {
+    SolverDev &s = sv->s;
+    const MeshDev &m = sv->mesh->d;
+    StageArgs a;
+    a.E = m.num_elem;
+    a.mode = mode;
+    a.flux = s.flux;
+    a.gamma = s.gamma;
+    a.ax = s.ax;
+    a.ay = s.ay;
+    a.gammaf = static_cast<float>(s.gamma);
+    a.axf = static_cast<float>(s.ax);
+    a.ayf = static_cast<float>(s.ay);
+    // plane starts are 16-byte aligned when E * sizeof(value) is a multiple of 16
+    a.prefetch = s.prefetch && (static_cast<size_t>(m.num_elem) * elem_size(s)) % 16 == 0 &&
+                 mode >= 2 && c && acc;
+    a.status = s.status;
+    a.u = u;
+    a.c = c;
+    a.acc = acc;
+    a.out = out;
+    a.nbr = m.nbr;
+    a.halo_off = m.halo_off;
+    a.halo_list = m.halo_list;
+    a.nslot = (3 * kTile + m.max_halo + 3) & ~3;   // keeps the prefetch area 16-byte aligned
+    a.scal = s.scal;
+    a.dt = dt;
+    a.t = t;
+    if (s.precision == DGX_FP64) {
+        a.geo = m.geo64;
+        a.fn = m.fn64;
+    } else {
+        a.geo = m.geo32;
+        a.fn = m.fn32;
+    }
+    return a;
+}
 
 void set_error(const char *fmt, ...) {
     va_list ap;
@@ -567,6 +579,7 @@ int dgx_run(dgx_solver *sv, double t_end, int max_steps, int *steps, double *t, 
         DGX_TRY_CUDA(cudaMemcpyAsync(&sn, sv->s.steps, sizeof(sn), cudaMemcpyDeviceToHost, st));
         DGX_TRY_CUDA(cudaMemcpyAsync(&status, sv->s.status, sizeof(status), cudaMemcpyDeviceToHost, st));
         DGX_TRY_CUDA(cudaStreamSynchronize(st));
+        if (status & kStatusCopyTimeout) { set_error("a bounded wait for an asynchronous copy ran out"); return DGX_ERR_TIMEOUT; }
         if (status) { set_error("state became non-finite or unphysical (flags %u)", status); return DGX_ERR_NONFINITE; }
         const bool done_t = t_end > 0.0 && (h[1] >= t_end || h[0] == 0.0);
         const bool done_n = max_steps > 0 && issued >= max_steps;
@@ -583,6 +596,14 @@ int dgx_conserved_totals(dgx_solver *sv, double *out, void *stream) {
     int rc = conserved_totals(sv->s, sv->mesh->d, out, as_stream(stream));
     if (!rc) sv->launches += 2 * sv->s.nv * 2;
     return rc;
+}
+
+int dgx_solver_set_option(dgx_solver *sv, int option, int value) {
+    if (!sv) return DGX_ERR_INVALID;
+    switch (option) {
+    case DGX_OPT_PREFETCH: sv->s.prefetch = value ? 1 : 0; return DGX_OK;
+    default: set_error("unknown option %d", option); return DGX_ERR_INVALID;
+    }
 }
 
 int dgx_max_wave_speed(dgx_solver *sv, double *out, void *stream) {

@@ -1,0 +1,398 @@
+// dgx_batch.cu -- many independent solves advanced together.
+//
+// Solves are grouped into classes of equal (precision, order, equation).  Each
+// class has work lists of (solve, element tile) items and one batched stage
+// kernel per RK stage walks them, so solves of uneven sizes share every launch.
+// One batched CFL kernel computes every solve's dt.  A time step -- the CFL
+// launch, then per class its four stage launches on its own stream -- is
+// captured once as a CUDA graph and replayed.  Per class, the kernel options
+// (TMA prefetch of the epilogue operands, flat or persistent grid) are chosen
+// by timing (dgx_batch_autotune).  This generalises the reference's one-solve
+// loop (src/2d/conservation/time_integrator.cu:252-429); it has no counterpart
+// there.
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "dgx_internal.h"
+
+namespace dgx {
+namespace {
+
+struct BatchClass {
+    int precision = 0, order = 0, equation = 0;
+    std::vector<int> solves;                 // indices into the batch's solver list
+    StageArgs *d_args[4] = {nullptr, nullptr, nullptr, nullptr};
+    int2 *d_items = nullptr;
+    int n_items = 0;
+    int nslot = 0;
+    int prefetch = 1;                        // tuned option
+    int persistent = 0;                      // tuned option: 0 flat grid, k > 0: k CTAs per SM
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    long long dofs = 0;
+};
+
+int num_sms() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    return sms;
+}
+
+}  // namespace
+}  // namespace dgx
+
+using namespace dgx;
+
+struct dgx_batch {
+    std::vector<dgx_solver *> solvers;
+    std::vector<BatchClass> classes;
+    DtArgs *d_dt = nullptr;
+    int2 *d_cfl_items = nullptr;
+    int n_cfl_items = 0;
+    cudaStream_t cap = nullptr;
+    cudaEvent_t start = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long dofs = 0;
+    long long launches = 0;
+    long long launches_per_step = 0;
+};
+
+namespace dgx {
+namespace {
+
+int class_launch(dgx_batch *b, BatchClass &k, int stage, cudaStream_t st) {
+    BatchStageArgs a;
+    a.args = k.d_args[stage];
+    a.items = k.d_items;
+    a.n_items = k.n_items;
+    a.nslot = k.nslot;
+    a.prefetch = stage >= 1 ? k.prefetch : 0;
+    if (k.persistent > 0) a.grid = std::min(k.n_items, num_sms() * k.persistent);
+    else a.grid = k.n_items;
+    const int rc = k.precision == DGX_FP64 ? launch_batch_stage_f64(k.order, k.equation, a, st)
+                                           : launch_batch_stage_f32(k.order, k.equation, a, st);
+    if (!rc && a.grid > 0) b->launches++;
+    return rc;
+}
+
+// Upload the per-solve stage arguments of one class for the given options.
+int class_upload(dgx_batch *b, BatchClass &k) {
+    std::vector<StageArgs> host(k.solves.size());
+    int nslot = 0;
+    for (int stage = 0; stage < 4; ++stage) {
+        for (size_t j = 0; j < k.solves.size(); ++j) {
+            dgx_solver *sv = b->solvers[k.solves[j]];
+            SolverDev &s = sv->s;
+            const int saved = s.prefetch;
+            s.prefetch = k.prefetch;
+            switch (stage) {
+            case 0: host[j] = make_stage_args(sv, 1, s.c, s.c, s.acc, s.ua, 0.0, 0.0); break;
+            case 1: host[j] = make_stage_args(sv, 2, s.ua, s.c, s.acc, s.ub, 0.0, 0.0); break;
+            case 2: host[j] = make_stage_args(sv, 3, s.ub, s.c, s.acc, s.ua, 0.0, 0.0); break;
+            default: host[j] = make_stage_args(sv, 4, s.ua, s.c, s.acc, s.c, 0.0, 0.0); break;
+            }
+            s.prefetch = saved;
+            nslot = std::max(nslot, host[j].nslot);
+        }
+        DGX_TRY_CUDA(cudaMemcpy(k.d_args[stage], host.data(), host.size() * sizeof(StageArgs),
+                                cudaMemcpyHostToDevice));
+    }
+    k.nslot = nslot;
+    // refuse a prefetch that would not fit in shared memory
+    const size_t smem = k.precision == DGX_FP64 ? batch_smem_f64(k.order, k.equation, nslot, k.prefetch)
+                                                : batch_smem_f32(k.order, k.equation, nslot, k.prefetch);
+    if (k.prefetch && smem > 200 * 1024) {
+        k.prefetch = 0;
+        return class_upload(b, k);
+    }
+    // set the kernel's shared-memory limit outside any capture (grid 0: no launch)
+    BatchStageArgs probe{k.d_args[1], k.d_items, 0, 0, k.nslot, k.prefetch};
+    int rc = k.precision == DGX_FP64 ? launch_batch_stage_f64(k.order, k.equation, probe, nullptr)
+                                     : launch_batch_stage_f32(k.order, k.equation, probe, nullptr);
+    return rc;
+}
+
+// one step without the graph
+int step_direct(dgx_batch *b, cudaStream_t st) {
+    int rc = launch_batch_dt(b->d_dt, b->d_cfl_items, b->n_cfl_items, st);
+    if (rc) return rc;
+    b->launches++;
+    for (auto &k : b->classes)
+        for (int stage = 0; stage < 4; ++stage) {
+            rc = class_launch(b, k, stage, st);
+            if (rc) return rc;
+        }
+    return DGX_OK;
+}
+
+void destroy_graph(dgx_batch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+// Capture one step: CFL on the capture stream, then each class's four stages on
+// its own stream (classes are independent), joined back.
+int build_graph(dgx_batch *b) {
+    destroy_graph(b);
+    const long long l0 = b->launches;
+    DGX_TRY_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+    int rc = launch_batch_dt(b->d_dt, b->d_cfl_items, b->n_cfl_items, b->cap);
+    b->launches++;
+    if (!rc) rc = cudaEventRecord(b->start, b->cap) == cudaSuccess ? DGX_OK : DGX_ERR_CUDA;
+    for (auto &k : b->classes) {
+        if (rc) break;
+        if (cudaStreamWaitEvent(k.stream, b->start, 0) != cudaSuccess) { rc = DGX_ERR_CUDA; break; }
+        for (int stage = 0; stage < 4 && !rc; ++stage) rc = class_launch(b, k, stage, k.stream);
+        if (!rc && cudaEventRecord(k.done, k.stream) != cudaSuccess) rc = DGX_ERR_CUDA;
+        if (!rc && cudaStreamWaitEvent(b->cap, k.done, 0) != cudaSuccess) rc = DGX_ERR_CUDA;
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(b->cap, &g);
+    if (rc || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (!rc) set_error("graph capture failed: %s", cudaGetErrorString(ce));
+        return rc ? rc : DGX_ERR_CUDA;
+    }
+    b->graph = g;
+    DGX_TRY_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
+    b->launches_per_step = b->launches - l0;
+    b->launches = l0;
+    return DGX_OK;
+}
+
+void batch_free(dgx_batch *b) {
+    destroy_graph(b);
+    for (auto &k : b->classes) {
+        for (auto p : k.d_args)
+            if (p) cudaFree(p);
+        if (k.d_items) cudaFree(k.d_items);
+        if (k.stream) cudaStreamDestroy(k.stream);
+        if (k.done) cudaEventDestroy(k.done);
+    }
+    if (b->d_dt) cudaFree(b->d_dt);
+    if (b->d_cfl_items) cudaFree(b->d_cfl_items);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    if (b->start) cudaEventDestroy(b->start);
+    delete b;
+}
+
+}  // namespace
+}  // namespace dgx
+
+extern "C" {
+
+int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
+    if (!solvers || n <= 0 || !out) { set_error("need at least one solver"); return DGX_ERR_INVALID; }
+    *out = nullptr;
+    dgx_batch *b = new (std::nothrow) dgx_batch();
+    if (!b) { set_error("host allocation failed"); return DGX_ERR_NOMEM; }
+    for (int i = 0; i < n; ++i) {
+        if (!solvers[i]) { set_error("solver %d is NULL", i); batch_free(b); return DGX_ERR_INVALID; }
+        for (int j = 0; j < i; ++j)
+            if (solvers[j] == solvers[i]) { set_error("solver %d appears twice", i); batch_free(b); return DGX_ERR_INVALID; }
+        b->solvers.push_back(solvers[i]);
+    }
+    // classes
+    for (int i = 0; i < n; ++i) {
+        const SolverDev &s = solvers[i]->s;
+        BatchClass *k = nullptr;
+        for (auto &c : b->classes)
+            if (c.precision == s.precision && c.order == s.order && c.equation == s.equation) k = &c;
+        if (!k) {
+            b->classes.emplace_back();
+            k = &b->classes.back();
+            k->precision = s.precision;
+            k->order = s.order;
+            k->equation = s.equation;
+        }
+        k->solves.push_back(i);
+        k->dofs += static_cast<long long>(s.n);
+        b->dofs += static_cast<long long>(s.n);
+    }
+    int rc = DGX_OK;
+    std::vector<DtArgs> dts(n);
+    std::vector<int2> cfl_items;
+    for (int i = 0; i < n; ++i) {
+        dts[i] = make_dt_args(solvers[i]->s, solvers[i]->mesh->d);
+        for (int blk = 0; blk < dts[i].nblocks; ++blk) cfl_items.push_back(make_int2(i, blk));
+    }
+    b->n_cfl_items = static_cast<int>(cfl_items.size());
+    if (cudaMalloc(&b->d_dt, sizeof(DtArgs) * n) != cudaSuccess ||
+        cudaMalloc(&b->d_cfl_items, sizeof(int2) * cfl_items.size()) != cudaSuccess) {
+        set_error("cudaMalloc failed");
+        batch_free(b);
+        return DGX_ERR_NOMEM;
+    }
+    if (cudaMemcpy(b->d_dt, dts.data(), sizeof(DtArgs) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(b->d_cfl_items, cfl_items.data(), sizeof(int2) * cfl_items.size(),
+                   cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_error("batch upload failed");
+        batch_free(b);
+        return DGX_ERR_CUDA;
+    }
+    for (auto &k : b->classes) {
+        std::vector<int2> items;
+        for (size_t j = 0; j < k.solves.size(); ++j) {
+            const int ntiles = b->solvers[k.solves[j]]->mesh->d.num_tiles;
+            for (int t = 0; t < ntiles; ++t) items.push_back(make_int2(static_cast<int>(j), t));
+        }
+        k.n_items = static_cast<int>(items.size());
+        for (auto &p : k.d_args)
+            if (cudaMalloc(&p, sizeof(StageArgs) * k.solves.size()) != cudaSuccess) rc = DGX_ERR_NOMEM;
+        if (!rc && cudaMalloc(&k.d_items, sizeof(int2) * items.size()) != cudaSuccess) rc = DGX_ERR_NOMEM;
+        if (!rc && cudaMemcpy(k.d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice) !=
+                       cudaSuccess)
+            rc = DGX_ERR_CUDA;
+        if (!rc && (cudaStreamCreateWithFlags(&k.stream, cudaStreamNonBlocking) != cudaSuccess ||
+                    cudaEventCreateWithFlags(&k.done, cudaEventDisableTiming) != cudaSuccess))
+            rc = DGX_ERR_CUDA;
+        if (!rc) rc = class_upload(b, k);
+        if (rc) break;
+    }
+    if (!rc && (cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess ||
+                cudaEventCreateWithFlags(&b->start, cudaEventDisableTiming) != cudaSuccess))
+        rc = DGX_ERR_CUDA;
+    if (!rc) rc = build_graph(b);
+    if (rc) {
+        if (!dgx_last_error()[0]) set_error("batch creation failed");
+        batch_free(b);
+        return rc;
+    }
+    *out = b;
+    return DGX_OK;
+}
+
+int dgx_batch_destroy(dgx_batch *b) {
+    if (!b) return DGX_ERR_INVALID;
+    cudaDeviceSynchronize();
+    batch_free(b);
+    return DGX_OK;
+}
+
+int dgx_batch_step(dgx_batch *b, void *stream) {
+    if (!b || !b->exec) return DGX_ERR_INVALID;
+    DGX_TRY_CUDA(cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)));
+    b->launches += b->launches_per_step;
+    return DGX_OK;
+}
+
+int dgx_batch_run(dgx_batch *b, int steps, void *stream) {
+    if (!b || steps < 0) return DGX_ERR_INVALID;
+    for (int i = 0; i < steps; ++i) {
+        int rc = dgx_batch_step(b, stream);
+        if (rc) return rc;
+    }
+    return DGX_OK;
+}
+
+int dgx_batch_info(const dgx_batch *b, int *num_classes, int *num_items, long long *dofs,
+                   long long *launches_per_step) {
+    if (!b) return DGX_ERR_INVALID;
+    int items = 0;
+    for (auto &k : b->classes) items += k.n_items;
+    if (num_classes) *num_classes = static_cast<int>(b->classes.size());
+    if (num_items) *num_items = items;
+    if (dofs) *dofs = b->dofs;
+    if (launches_per_step) *launches_per_step = b->launches_per_step;
+    return DGX_OK;
+}
+
+int dgx_batch_class_options(const dgx_batch *b, int cls, int *order, int *equation, int *prefetch,
+                            int *persistent) {
+    if (!b || cls < 0 || cls >= static_cast<int>(b->classes.size())) return DGX_ERR_INVALID;
+    const auto &k = b->classes[cls];
+    if (order) *order = k.order;
+    if (equation) *equation = k.equation;
+    if (prefetch) *prefetch = k.prefetch;
+    if (persistent) *persistent = k.persistent;
+    return DGX_OK;
+}
+
+int dgx_batch_launch_count(const dgx_batch *b, long long *count) {
+    if (!b || !count) return DGX_ERR_INVALID;
+    *count = b->launches;
+    return DGX_OK;
+}
+
+// Time the candidate options of every class on the live batch, keep the
+// fastest, and rebuild the graph.  The solves' states, times and step counts
+// are saved before and restored after, so the batch continues as if untuned.
+int dgx_batch_autotune(dgx_batch *b, int reps, void *stream) {
+    if (!b) return DGX_ERR_INVALID;
+    if (reps <= 0) reps = 3;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    DGX_TRY_CUDA(cudaStreamSynchronize(st));
+    // save
+    const size_t n = b->solvers.size();
+    std::vector<void *> saved(n, nullptr);
+    std::vector<double> scal(8 * n);
+    std::vector<long long> steps(n);
+    int rc = DGX_OK;
+    for (size_t i = 0; i < n && !rc; ++i) {
+        SolverDev &s = b->solvers[i]->s;
+        const size_t bytes = s.n * (s.precision == DGX_FP64 ? 8 : 4);
+        if (cudaMalloc(&saved[i], bytes) != cudaSuccess) { set_error("autotune backup allocation failed"); rc = DGX_ERR_NOMEM; break; }
+        if (cudaMemcpy(saved[i], s.c, bytes, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+            cudaMemcpy(&scal[8 * i], s.scal, 8 * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(&steps[i], s.steps, sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = DGX_ERR_CUDA;
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) rc = DGX_ERR_CUDA;
+    // one CFL launch gives every solve a dt for the timed stage launches
+    if (!rc) rc = launch_batch_dt(b->d_dt, b->d_cfl_items, b->n_cfl_items, st);
+    const int cand[][2] = {{1, 0}, {0, 0}, {1, 2}, {0, 2}, {1, 4}};
+    for (auto &k : b->classes) {
+        if (rc) break;
+        float best = 1e30f;
+        int bp = k.prefetch, bq = k.persistent;
+        for (auto &c : cand) {
+            k.prefetch = c[0];
+            k.persistent = c[1];
+            rc = class_upload(b, k);
+            if (rc) break;
+            if (c[0] && !k.prefetch) continue;    // prefetch does not fit
+            for (int w = 0; w < 1 && !rc; ++w)
+                for (int stage = 1; stage < 4 && !rc; ++stage) rc = class_launch(b, k, stage, st);
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < reps && !rc; ++r)
+                for (int stage = 1; stage < 4 && !rc; ++stage) rc = class_launch(b, k, stage, st);
+            cudaEventRecord(e1, st);
+            if (rc) break;
+            if (cudaEventSynchronize(e1) != cudaSuccess) { rc = DGX_ERR_CUDA; break; }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) { best = ms; bp = c[0]; bq = c[1]; }
+        }
+        k.prefetch = bp;
+        k.persistent = bq;
+        if (!rc) rc = class_upload(b, k);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    // restore
+    for (size_t i = 0; i < n; ++i) {
+        SolverDev &s = b->solvers[i]->s;
+        if (!saved[i]) continue;
+        const size_t bytes = s.n * (s.precision == DGX_FP64 ? 8 : 4);
+        if (cudaMemcpy(s.c, saved[i], bytes, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+            cudaMemcpy(s.scal, &scal[8 * i], 8 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(s.steps, &steps[i], sizeof(long long), cudaMemcpyHostToDevice) != cudaSuccess)
+            rc = rc ? rc : DGX_ERR_CUDA;
+        cudaFree(saved[i]);
+    }
+    if (!rc) rc = build_graph(b);
+    return rc;
+}
+
+}  // extern "C"

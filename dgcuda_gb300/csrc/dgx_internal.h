@@ -38,6 +38,7 @@ void set_error(const char *fmt, ...);
 enum StatusBits : unsigned int {
     kStatusNonFinite = 1u,   // NaN/Inf wave speed or state
     kStatusNegative = 2u,    // non-positive density or pressure in a cell average
+    kStatusCopyTimeout = 4u, // a bounded wait for an asynchronous copy ran out
 };
 
 // Elements are processed in tiles of kTile consecutive elements, one CTA per
@@ -101,6 +102,7 @@ struct SolverDev {
     double *red = nullptr;             // reduction scratch (partials)
     int red_len = 0;
     int dt_mode = DGX_DT_CFL;
+    int prefetch = 1;                  // DGX_OPT_PREFETCH
 };
 
 }  // namespace dgx
@@ -124,6 +126,9 @@ struct StageArgs {
     int mode;          // 0 rhs, 1..4 RK4 stages
     int flux;
     double gamma, ax, ay;
+    float gammaf, axf, ayf;   // the same in FP32 (FP32 kernels)
+    int prefetch;      // 1: copy the epilogue operands with the TMA engine (needs 16-byte aligned planes)
+    unsigned int *status;
     const void *u;     // stage input (read-only)
     const void *c;     // base state
     void *acc;         // accumulator
@@ -138,8 +143,41 @@ struct StageArgs {
     double dt, t;         // host dt/t for mode 0
 };
 
+// Batched launch: items[i] = (index into args, tile); grid CTAs walk the list.
+struct BatchStageArgs {
+    const StageArgs *args;   // device array, one per solve of the class
+    const int2 *items;       // device array of (solve, tile)
+    int n_items;
+    int grid;
+    int nslot;               // largest nslot of the class (shared-memory size)
+    int prefetch;            // any solve of the class prefetches
+};
+
 int launch_stage_f32(int order, int equation, const StageArgs &a, cudaStream_t st);
+int launch_batch_stage_f32(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
+int launch_batch_stage_f64(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
+size_t batch_smem_f32(int order, int equation, int nslot, int prefetch);
+size_t batch_smem_f64(int order, int equation, int nslot, int prefetch);
 int launch_stage_f64(int order, int equation, const StageArgs &a, cudaStream_t st);
+
+// per-solve time-step arguments (dgx_misc.cu)
+struct DtArgs {
+    const void *c;
+    int E, np, is_double, euler, cfl_mode, order;
+    double gamma, phi0, amax, min_diam;
+    double *scal;
+    unsigned long long *lam_bits;
+    unsigned int *counter, *status;
+    long long *steps;
+    int nblocks;      // blocks that reduce this solve's wave speeds
+};
+DtArgs make_dt_args(const SolverDev &s, const MeshDev &m);
+// batched CFL: items[i] = (solve, block of that solve)
+int launch_batch_dt(const DtArgs *args, const int2 *items, int n_items, cudaStream_t st);
+
+// per-solve stage arguments (dgx_api.cu)
+StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c, void *acc,
+                          void *out, double dt, double t);
 
 // misc kernels (dgx_misc.cu)
 int mesh_geometry(MeshDev &m, cudaStream_t st);

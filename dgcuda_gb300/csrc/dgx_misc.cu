@@ -203,16 +203,6 @@ __global__ void project_kernel(MeshDev m, const Tables *tabs, int p, int nv, int
 // (time_integrator.cu:252-270).  The last block to finish computes dt, so the
 // whole step stays on the device.
 // ---------------------------------------------------------------------------
-struct DtArgs {
-    const void *c;
-    int E, np, is_double, euler, cfl_mode, order;
-    double gamma, phi0, amax, min_diam;
-    double *scal;
-    unsigned long long *lam_bits;
-    unsigned int *counter, *status;
-    long long *steps;
-};
-
 __device__ void finish_dt(const DtArgs &a, double lam) {
     double *sc = a.scal;
     const double t = sc[1], t_end = sc[5];
@@ -236,14 +226,14 @@ __device__ void finish_dt(const DtArgs &a, double lam) {
 }
 
 template <typename T>
-__global__ void cfl_kernel(DtArgs a) {
+__device__ void cfl_block(const DtArgs &a, int block, int nblocks) {
     __shared__ double sh[kThreads / 32];
     double lmax = 0.0;
     unsigned int bad = 0;
     if (a.euler) {
         const T *c = static_cast<const T *>(a.c);
         const size_t SE = a.E, NPE = static_cast<size_t>(a.np) * SE;
-        for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < a.E; e += gridDim.x * blockDim.x) {
+        for (int e = block * blockDim.x + threadIdx.x; e < a.E; e += nblocks * blockDim.x) {
             const double rho = static_cast<double>(c[e]) * a.phi0;
             const double ru = static_cast<double>(c[NPE + e]) * a.phi0;
             const double rv = static_cast<double>(c[2 * NPE + e]) * a.phi0;
@@ -268,7 +258,7 @@ __global__ void cfl_kernel(DtArgs a) {
         atomicMax(a.lam_bits, static_cast<unsigned long long>(__double_as_longlong(m)));
         __threadfence();
         const unsigned int done = atomicAdd(a.counter, 1u);
-        if (done == gridDim.x - 1) {
+        if (done == static_cast<unsigned>(nblocks) - 1) {
             __threadfence();
             const double lam = a.euler ? __longlong_as_double(static_cast<long long>(atomicAdd(a.lam_bits, 0ull)))
                                        : a.amax;
@@ -277,6 +267,21 @@ __global__ void cfl_kernel(DtArgs a) {
             *a.lam_bits = 0ull;
             *a.counter = 0u;
         }
+    }
+}
+
+template <typename T>
+__global__ void cfl_kernel(DtArgs a) {
+    cfl_block<T>(a, blockIdx.x, gridDim.x);
+}
+
+__global__ void batch_cfl_kernel(const DtArgs *args, const int2 *items, int n_items) {
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const int2 w = items[it];
+        const DtArgs a = args[w.x];
+        if (a.is_double) cfl_block<double>(a, w.y, a.nblocks);
+        else cfl_block<float>(a, w.y, a.nblocks);
+        __syncthreads();
     }
 }
 
@@ -347,7 +352,7 @@ int project_ic(const SolverDev &s, const MeshDev &m, int ic, const double *param
     return DGX_OK;
 }
 
-int launch_dt(SolverDev &s, const MeshDev &m, cudaStream_t st) {
+DtArgs make_dt_args(const SolverDev &s, const MeshDev &m) {
     DtArgs a;
     a.c = s.c;
     a.E = m.num_elem;
@@ -365,13 +370,25 @@ int launch_dt(SolverDev &s, const MeshDev &m, cudaStream_t st) {
     a.counter = s.counter;
     a.status = s.status;
     a.steps = s.steps;
-    int grid = 1;
+    a.nblocks = 1;
     if (a.euler) {
-        grid = blocks_for(m.num_elem);
-        if (grid > 152 * 8) grid = 152 * 8;
+        a.nblocks = blocks_for(m.num_elem);
+        if (a.nblocks > 152 * 8) a.nblocks = 152 * 8;
     }
-    if (a.is_double) cfl_kernel<double><<<grid, kThreads, 0, st>>>(a);
-    else cfl_kernel<float><<<grid, kThreads, 0, st>>>(a);
+    return a;
+}
+
+int launch_dt(SolverDev &s, const MeshDev &m, cudaStream_t st) {
+    const DtArgs a = make_dt_args(s, m);
+    if (a.is_double) cfl_kernel<double><<<a.nblocks, kThreads, 0, st>>>(a);
+    else cfl_kernel<float><<<a.nblocks, kThreads, 0, st>>>(a);
+    DGX_CHECK_LAUNCH();
+    return DGX_OK;
+}
+
+int launch_batch_dt(const DtArgs *args, const int2 *items, int n_items, cudaStream_t st) {
+    int grid = n_items < 152 * 16 ? n_items : 152 * 16;
+    if (grid > 0) batch_cfl_kernel<<<grid, kThreads, 0, st>>>(args, items, n_items);
     DGX_CHECK_LAUNCH();
     return DGX_OK;
 }

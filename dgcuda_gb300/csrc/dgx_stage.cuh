@@ -48,10 +48,49 @@ struct Lay {
 
 using R = DGX_REAL;
 
-__device__ __forceinline__ R rrcp(float x) { return __frcp_rn(x); }
-__device__ __forceinline__ R rrcp(double x) { return 1.0 / x; }
-__device__ __forceinline__ R rsqrt_(float x) { return sqrtf(x); }
-__device__ __forceinline__ R rsqrt_(double x) { return sqrt(x); }
+// FP32: the SFU reciprocal and reciprocal square root (a few ulp, far inside
+// the FP32 path's tolerance); FP64: IEEE division and square root.
+__device__ __forceinline__ float rrcp(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double rrcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float rsqrt_(float x) { return x * rsqrtf(x); }   // x > 0
+__device__ __forceinline__ double rsqrt_(double x) { return sqrt(x); }
+
+// ---- bulk asynchronous copies (TMA engine) into shared memory -------------
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+// global -> shared, 16-byte aligned addresses, size a multiple of 16
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes,
+                                              unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the phase with the given parity: false if the limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar, unsigned parity, long long limit) {
+    for (long long it = 0; it < limit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
 
 // Physical flux (Fx, Fy) at a point: advection a*u, Euler
 // (src/2d/conservation/euler/euler.cu:92-117).
@@ -110,40 +149,82 @@ __device__ __forceinline__ void num_flux(const R *UL, const R *UR, R nx, R ny, i
 template <int P, int NV>
 DGX_HD constexpr int side_table_words() { return (3 * num_modes(P) * num_quad1(P) + 3) & ~3; }
 
+// bytes of the prefetched epilogue operands (base state and accumulator slices
+// of the tile: 2 x NV x NP planes of kTile values)
 template <int P, int NV>
-DGX_HD constexpr size_t stage_smem_bytes(int nslot) {
-    return sizeof(R) * (static_cast<size_t>(side_table_words<P, NV>()) +
-                        static_cast<size_t>(NV) * num_quad1(P) * nslot);
+DGX_HD constexpr size_t prefetch_bytes() {
+    return sizeof(R) * 2 * NV * num_modes(P) * kTile;
 }
 
+template <int P, int NV>
+DGX_HD constexpr size_t stage_smem_bytes(int nslot, int prefetch) {
+    return 16 + sizeof(R) * (static_cast<size_t>(side_table_words<P, NV>()) +
+                             static_cast<size_t>(NV) * num_quad1(P) * nslot) +
+           (prefetch ? prefetch_bytes<P, NV>() : 0);
+}
+
+// One tile of one solve.  `bar` is an initialised mbarrier; `parity` the phase
+// this tile's prefetch (if any) completes; returns whether a prefetch was
+// issued (the caller then advances its phase).  All threads of the CTA call it
+// with the same arguments; on return no copy of this tile is in flight.
 template <int P, int EQ>
-__global__ void __launch_bounds__(kTile, (P <= 3 ? 4 : 2)) stage_kernel(const StageArgs a) {
+__device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, unsigned char *smem_raw,
+                                           const unsigned parity) {
     using L = Lay<P>;
     constexpr int NP = L::NP, NQ = L::NQ, NQ1 = L::NQ1;
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    R *s_side = reinterpret_cast<R *>(smem_raw);
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem_raw);
+    R *s_side = reinterpret_cast<R *>(smem_raw + 16);
     R *s_tr = s_side + side_table_words<P, NV>();
     const int nslot = a.nslot;
+    // epilogue operands (base state, accumulator) of the tile, prefetched by the
+    // TMA engine while the element work runs; 16-byte aligned (side_table_words
+    // is a multiple of 4 and nslot of kTile-sized planes keeps alignment)
+    R *s_pre = s_tr + static_cast<size_t>(NV) * NQ1 * nslot;
 
     R dt;
     if (a.mode == 0) {
         dt = R(a.dt);
     } else {
         dt = R(a.scal[0]);
-        if (dt == R(0)) return;   // the run has reached its end time (uniform over the grid)
+        if (dt == R(0)) return false;   // the run has reached its end time (uniform over the CTA)
     }
     const int E = a.E;
     const int tid = threadIdx.x;
-    const int tile = blockIdx.x;
     const int e = tile * kTile + tid;
     const bool live = e < E;
     const size_t SE = static_cast<size_t>(E);
-    const R g = R(a.gamma), ax = R(a.ax), ay = R(a.ay);
+    // physics constants in the kernel's precision (FP32 copies avoid FP64 conversions)
+    const R g = sizeof(R) == 4 ? R(a.gammaf) : R(a.gamma);
+    const R ax = sizeof(R) == 4 ? R(a.axf) : R(a.ax);
+    const R ay = sizeof(R) == 4 ? R(a.ayf) : R(a.ay);
     const int llf = a.flux == DGX_FLUX_LLF;
     const R *__restrict__ u = static_cast<const R *>(a.u);
 
     for (int t = tid; t < 3 * NP * NQ1; t += kTile) s_side[t] = c_tab[L::SIDE + t];
+
+    // modes 2..4 read the base state (2, 3) and the accumulator (2, 3, 4) at the
+    // end: start their copies now
+    const bool pre = a.prefetch && a.mode >= 2;
+    if (pre && tid < 32) {
+        // order this CTA's earlier generic-proxy accesses of the shared memory
+        // (a previous tile) before the bulk copies that overwrite it
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const int cnt = min(kTile, E - tile * kTile);
+        const unsigned bytes = static_cast<unsigned>(cnt * sizeof(R));
+        const int nplanes = NV * NP;
+        const int ncopy = (a.mode == 4) ? nplanes : 2 * nplanes;
+        if (tid == 0) mbar_expect_tx(bar, bytes * ncopy);
+        __syncwarp();
+        for (int q = tid; q < ncopy; q += 32) {
+            // planes [0, nplanes): base state (modes 2, 3), then the accumulator;
+            // mode 4 copies only the accumulator, to planes [0, nplanes)
+            const int which = (a.mode == 4) ? 1 : (q >= nplanes);
+            const int pl = q % nplanes;
+            const R *src = static_cast<const R *>(which ? a.acc : a.c) + pl * SE + static_cast<size_t>(tile) * kTile;
+            bulk_copy_g2s(s_pre + static_cast<size_t>(q) * kTile, src, bytes, bar);
+        }
+    }
 
     // own coefficients (coalesced: 32 consecutive elements per warp and (n,i))
     R c[NV][NP];
@@ -151,6 +232,22 @@ __global__ void __launch_bounds__(kTile, (P <= 3 ? 4 : 2)) stage_kernel(const St
     for (int n = 0; n < NV; ++n)
 #pragma unroll
         for (int i = 0; i < NP; ++i) c[n][i] = live ? __ldg(u + (n * NP + i) * SE + e) : R(0);
+
+    // side data of the three sides
+    int sw[3];
+    R snx[3], sny[3], shl[3];
+    {
+        const int *__restrict__ nbr = a.nbr;
+        const R *__restrict__ fn = static_cast<const R *>(a.fn);
+        const int ee = live ? e : 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            sw[k] = __ldg(nbr + k * SE + ee);
+            snx[k] = __ldg(fn + (3 * k + 0) * SE + ee);
+            sny[k] = __ldg(fn + (3 * k + 1) * SE + ee);
+            shl[k] = __ldg(fn + (3 * k + 2) * SE + ee);
+        }
+    }
 
     // first halo entry of this thread: issue its gathers before any compute
     const int h0 = __ldg(a.halo_off + tile), H = __ldg(a.halo_off + tile + 1) - h0;
@@ -190,15 +287,23 @@ __global__ void __launch_bounds__(kTile, (P <= 3 ? 4 : 2)) stage_kernel(const St
                 for (int i = 0; i < NP; ++i) cn[n][i] = __ldg(u + (n * NP + i) * SE + ne);
         }
         const R *ts = s_side + (hw & 3) * NP * NQ1;
+        R tr[NQ1][NV];
 #pragma unroll
         for (int j = 0; j < NQ1; ++j)
 #pragma unroll
-            for (int n = 0; n < NV; ++n) {
-                R s = R(0);
+            for (int n = 0; n < NV; ++n) tr[j][n] = R(0);
 #pragma unroll
-                for (int i = 0; i < NP; ++i) s = fma(cn[n][i], ts[i * NQ1 + j], s);
-                s_tr[(j * NV + n) * nslot + 3 * kTile + h] = s;
+        for (int i = 0; i < NP; ++i)
+#pragma unroll
+            for (int j = 0; j < NQ1; ++j) {
+                const R t = ts[i * NQ1 + j];
+#pragma unroll
+                for (int n = 0; n < NV; ++n) tr[j][n] = fma(cn[n][i], t, tr[j][n]);
             }
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j)
+#pragma unroll
+            for (int n = 0; n < NV; ++n) s_tr[(j * NV + n) * nslot + 3 * kTile + h] = tr[j][n];
     }
 
     R rhs[NV][NP];
@@ -236,17 +341,16 @@ __global__ void __launch_bounds__(kTile, (P <= 3 ? 4 : 2)) stage_kernel(const St
         }
     }
     __syncthreads();   // all traces of the tile and its halo are in shared memory
-    if (!live) return;
+    if (!live) {
+        // this thread has no element; the CTA's copies are waited for by the others
+        return pre;
+    }
 
     // ---- the three sides --------------------------------------------------------
-    const int *__restrict__ nbr = a.nbr;
-    const R *__restrict__ fn = static_cast<const R *>(a.fn);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const int word = __ldg(nbr + k * SE + e);
-        const R nx = __ldg(fn + (3 * k + 0) * SE + e);
-        const R ny = __ldg(fn + (3 * k + 1) * SE + e);
-        const R hl = __ldg(fn + (3 * k + 2) * SE + e);
+        const int word = sw[k];
+        const R nx = snx[k], ny = sny[k], hl = shl[k];
         const int own = 3 * tid + k;
         // a boundary side (rejected at solver creation) would mirror the own trace
         const int slot = word >= 0 ? (word >> 1) : own;
@@ -279,6 +383,23 @@ __global__ void __launch_bounds__(kTile, (P <= 3 ? 4 : 2)) stage_kernel(const St
     // ---- mass inverse and RK combination ---------------------------------------
     const R sc = dt * invJ;
     R *__restrict__ out = static_cast<R *>(a.out);
+    const R *pc = nullptr, *pacc = nullptr;   // base state / accumulator of this element
+    size_t pstride = SE;
+    if (pre) {
+        if (!mbar_wait_bounded(bar, parity, 1ll << 26)) {
+            // the copies did not land in time: report, wait once more for the
+            // copies still in flight (they write this CTA's shared memory), skip
+            atomicOr(a.status, kStatusCopyTimeout);
+            mbar_wait_bounded(bar, parity, 1ll << 28);
+            return pre;
+        }
+        pc = s_pre + tid;
+        pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * kTile) + tid;
+        pstride = kTile;
+    } else {
+        pc = static_cast<const R *>(a.c) + e;
+        pacc = static_cast<const R *>(a.acc) + e;
+    }
     switch (a.mode) {
     case 0:
 #pragma unroll
@@ -301,7 +422,6 @@ __global__ void __launch_bounds__(kTile, (P <= 3 ? 4 : 2)) stage_kernel(const St
     }
     case 2:     // u3 = c + k2/2, acc += k2/3
     case 3: {   // u4 = c + k3,   acc += k3/3
-        const R *__restrict__ cb = static_cast<const R *>(a.c);
         R *__restrict__ acc = static_cast<R *>(a.acc);
         const R alpha = a.mode == 2 ? R(0.5) : R(1);
 #pragma unroll
@@ -310,29 +430,61 @@ __global__ void __launch_bounds__(kTile, (P <= 3 ? 4 : 2)) stage_kernel(const St
             for (int i = 0; i < NP; ++i) {
                 const R kk = sc * rhs[n][i];
                 const size_t o = (n * NP + i) * SE + e;
-                out[o] = fma(alpha, kk, __ldg(cb + o));
-                acc[o] = fma(R(1.0 / 3.0), kk, acc[o]);
+                const size_t po = (n * NP + i) * pstride;
+                out[o] = fma(alpha, kk, pc[po]);
+                acc[o] = fma(R(1.0 / 3.0), kk, pacc[po]);
             }
         break;
     }
     default: {  // c = acc + k4/6
-        const R *__restrict__ acc = static_cast<const R *>(a.acc);
 #pragma unroll
         for (int n = 0; n < NV; ++n)
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
                 const size_t o = (n * NP + i) * SE + e;
-                out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], acc[o]);
+                out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], pacc[(n * NP + i) * pstride]);
             }
         break;
     }
     }
+    return pre;
+}
+
+template <int P>
+constexpr int min_ctas() { return P <= 3 ? 4 : 2; }
+
+// Plain path: one CTA per tile of one solve.
+template <int P, int EQ>
+__global__ void __launch_bounds__(kTile, min_ctas<P>()) stage_kernel(const StageArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (threadIdx.x == 0) mbar_init(reinterpret_cast<unsigned long long *>(smem_raw), 1);
+    __syncthreads();
+    stage_tile<P, EQ>(a, blockIdx.x, smem_raw, 0u);
+}
+
+// Batched path: the CTAs of one launch walk a work list of (solve, tile) items
+// of many solves of the same order and equation (grid-stride, so the launch can
+// be persistent); every solve keeps its own state, geometry and dt.
+template <int P, int EQ>
+__global__ void __launch_bounds__(kTile, min_ctas<P>()) batch_stage_kernel(const BatchStageArgs b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (threadIdx.x == 0) mbar_init(reinterpret_cast<unsigned long long *>(smem_raw), 1);
+    __syncthreads();
+    unsigned phase = 0;
+    for (int it = blockIdx.x; it < b.n_items; it += gridDim.x) {
+        const int2 w = b.items[it];
+        const StageArgs a = b.args[w.x];
+        if (stage_tile<P, EQ>(a, w.y, smem_raw, phase & 1u)) ++phase;
+        __syncthreads();   // shared memory is reused by the next item
+    }
 }
 
 template <int P, int EQ>
-static int launch_one(const StageArgs &a, cudaStream_t st) {
+static int launch_one(const StageArgs &a_in, cudaStream_t st) {
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
-    const size_t smem = stage_smem_bytes<P, NV>(a.nslot);
+    StageArgs a = a_in;
+    if (a.prefetch && stage_smem_bytes<P, NV>(a.nslot, 1) > 200 * 1024) a.prefetch = 0;
+    const size_t smem = stage_smem_bytes<P, NV>(a.nslot, a.prefetch);
     static size_t configured = 0;   // dynamic shared memory opted in so far
     if (smem > 48 * 1024 && smem > configured) {
         DGX_TRY_CUDA(cudaFuncSetAttribute(stage_kernel<P, EQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -343,6 +495,48 @@ static int launch_one(const StageArgs &a, cudaStream_t st) {
     if (grid > 0) stage_kernel<P, EQ><<<grid, kTile, smem, st>>>(a);
     DGX_CHECK_LAUNCH();
     return DGX_OK;
+}
+
+template <int P, int EQ>
+static int launch_batch_one(const BatchStageArgs &b, cudaStream_t st) {
+    constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
+    const size_t smem = stage_smem_bytes<P, NV>(b.nslot, b.prefetch);
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel<P, EQ>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        configured = smem;
+    }
+    if (b.grid > 0) batch_stage_kernel<P, EQ><<<b.grid, kTile, smem, st>>>(b);
+    DGX_CHECK_LAUNCH();
+    return DGX_OK;
+}
+
+// bytes of dynamic shared memory one CTA of the batched kernel needs
+template <int EQ>
+static size_t batch_smem_impl(int order, int nslot, int prefetch) {
+    constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
+    switch (order) {
+    case 0: return stage_smem_bytes<0, NV>(nslot, prefetch);
+    case 1: return stage_smem_bytes<1, NV>(nslot, prefetch);
+    case 2: return stage_smem_bytes<2, NV>(nslot, prefetch);
+    case 3: return stage_smem_bytes<3, NV>(nslot, prefetch);
+    case 4: return stage_smem_bytes<4, NV>(nslot, prefetch);
+    default: return stage_smem_bytes<5, NV>(nslot, prefetch);
+    }
+}
+
+template <int EQ>
+static int launch_batch_order(int order, const BatchStageArgs &b, cudaStream_t st) {
+    switch (order) {
+    case 0: return launch_batch_one<0, EQ>(b, st);
+    case 1: return launch_batch_one<1, EQ>(b, st);
+    case 2: return launch_batch_one<2, EQ>(b, st);
+    case 3: return launch_batch_one<3, EQ>(b, st);
+    case 4: return launch_batch_one<4, EQ>(b, st);
+    case 5: return launch_batch_one<5, EQ>(b, st);
+    default: set_error("unsupported order %d", order); return DGX_ERR_UNSUPPORTED;
+    }
 }
 
 template <int EQ>

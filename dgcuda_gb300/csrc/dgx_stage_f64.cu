@@ -7,4 +7,12 @@ int launch_stage_f64(int order, int equation, const StageArgs &a, cudaStream_t s
     return launch_stage_impl(order, equation, a, st);
 }
 int upload_tables_f64() { return upload_tables_impl(); }
+int launch_batch_stage_f64(int order, int equation, const BatchStageArgs &b, cudaStream_t st) {
+    return equation == DGX_EULER ? launch_batch_order<DGX_EULER>(order, b, st)
+                                 : launch_batch_order<DGX_ADVECTION>(order, b, st);
+}
+size_t batch_smem_f64(int order, int equation, int nslot, int prefetch) {
+    return equation == DGX_EULER ? batch_smem_impl<DGX_EULER>(order, nslot, prefetch)
+                                 : batch_smem_impl<DGX_ADVECTION>(order, nslot, prefetch);
+}
 }  // namespace dgx

@@ -187,6 +187,9 @@ class Solver:
         call("dgx_max_wave_speed", self.h, C.byref(v), stream)
         return v.value
 
+    def set_option(self, option: int, value: int) -> None:
+        call("dgx_solver_set_option", self.h, int(option), int(value))
+
     def launch_count(self) -> int:
         v = C.c_longlong()
         call("dgx_launch_count", self.h, C.byref(v))

@@ -180,8 +180,41 @@ int dgx_conserved_totals_static(const dgx_solver *solver, const void *state, dou
                                 void *stream);
 /* Maximum cell-average wave speed of the resident state. */
 int dgx_max_wave_speed(dgx_solver *solver, double *out, void *stream);
+/* Kernel options of a solver (for autotuning and tests):
+ *   DGX_OPT_PREFETCH  1 (default): RK stages 2-4 copy the tile's base state and
+ *                     accumulator into shared memory with the TMA engine while
+ *                     the element work runs; 0: plain loads at the end. */
+enum dgx_option { DGX_OPT_PREFETCH = 1 };
+int dgx_solver_set_option(dgx_solver *solver, int option, int value);
 /* Number of CUDA kernels this solver has launched so far. */
 int dgx_launch_count(const dgx_solver *solver, long long *count);
+
+/* --- batches: many independent solves per launch --------------------------- */
+/* New, no counterpart in the reference (it runs one solve per process; this
+ * generalises its loop, src/2d/conservation/time_integrator.cu:252-429).
+ * Solves of equal (precision, order, equation) form a class; each RK stage
+ * launches one kernel per class over work lists of (solve, element tile), one
+ * batched kernel computes every solve's dt, and the whole step is captured as
+ * a CUDA graph.  Every solve keeps its own state, time, dt rule and end time
+ * (set them before creating the batch); each solve's result equals the same
+ * solve run alone with dgx_step, bit for bit.  Destroy the batch before its
+ * solvers. */
+typedef struct dgx_batch dgx_batch;
+int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out);
+int dgx_batch_destroy(dgx_batch *batch);
+/* one RK4 step of every solve (a graph launch, asynchronous on `stream`) */
+int dgx_batch_step(dgx_batch *batch, void *stream);
+int dgx_batch_run(dgx_batch *batch, int steps, void *stream);
+/* Choose per class, by timing `reps` stage launches on the live batch, the
+ * kernel options (TMA prefetch of the epilogue operands; flat grid or a
+ * persistent grid of 2 or 4 CTAs per SM), then rebuild the graph.  The solves'
+ * states and times are restored afterwards.  Synchronous. */
+int dgx_batch_autotune(dgx_batch *batch, int reps, void *stream);
+int dgx_batch_info(const dgx_batch *batch, int *num_classes, int *num_items, long long *dofs,
+                   long long *launches_per_step);
+int dgx_batch_class_options(const dgx_batch *batch, int cls, int *order, int *equation,
+                            int *prefetch, int *persistent);
+int dgx_batch_launch_count(const dgx_batch *batch, long long *count);
 
 #ifdef __cplusplus
 }

@@ -256,3 +256,20 @@ def test_config2_vortex_reduced(gpu, oracle_mod):
     n, t = sv.run(t_end=0.5)
     assert n == nref and abs(t - 0.5) < 1e-12
     assert rel_l2(sv.get_state(), ref).max() <= FP32_TOL
+
+
+@pytest.mark.parametrize("n", [8, 5], ids=["aligned", "unaligned"])
+def test_prefetch_option_is_bitwise_neutral(n, gpu):
+    """RK stages with the epilogue operands staged by the TMA engine give the
+    same bits as plain loads (E = 128: staged; E = 50: rows not 16-byte
+    aligned, so plain loads are used either way)."""
+    m, eq, ic, params = make_case("vortex", 3, n=n, seed=4)
+    out = []
+    for pre in (1, 0):
+        sv = Solver(m, 3, eq, _ffi.FLUX_LLF, _ffi.FP32)
+        sv.set_option(_ffi.OPT_PREFETCH, pre)
+        sv.project(ic, params)
+        sv.set_dt(None)
+        sv.run(max_steps=5)
+        out.append(sv.get_state())
+    np.testing.assert_array_equal(out[0], out[1])
