@@ -194,6 +194,142 @@ def cpu_baseline_sample(budget_s: float = 12.0):
                       f"periodic sub-problem ({mesh.num_elem} elements, p=3 Euler)"}
 
 
+def _config4_requests(seed: int, count: int, n_lo: int, n_hi: int):
+    """Solve specs drawn as in the batched configuration: equation 50/50, N
+    log-uniform in [n_lo, n_hi] (2N^2 triangles, jitter 0.15h), p uniform in
+    1..4, Gaussian pulses (width 0.05-0.2) for advection on [0,1]^2, isentropic
+    vortices (beta 1-5) for Euler on [0,10]^2, at random centres."""
+    from dgcuda_gb300 import _ffi
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        euler = rng.random() < 0.5
+        n = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi)))))
+        p = int(rng.integers(1, 5))
+        if euler:
+            params = (rng.uniform(0, 10), rng.uniform(0, 10), rng.uniform(1, 5), 1.0, 0.0, 10.0, 10.0)
+            out.append(dict(n=n, order=p, equation=_ffi.EULER, ic=_ffi.IC_VORTEX, params=params,
+                            lx=10.0, ly=10.0, jitter=0.15, seed=seed * 1000 + k))
+        else:
+            w = rng.uniform(0.05, 0.2)
+            params = (rng.uniform(0, 1), rng.uniform(0, 1), w * w, 1.0, 1.0)
+            out.append(dict(n=n, order=p, equation=_ffi.ADVECTION, ic=_ffi.IC_GAUSSIAN,
+                            params=params, lx=1.0, ly=1.0, jitter=0.15, seed=seed * 1000 + k))
+    return out
+
+
+def _native_solver(spec):
+    from dgcuda_gb300 import _ffi
+    from dgcuda_gb300.solver import DeviceMesh, Solver
+    dm = DeviceMesh.periodic_square(spec["n"], spec["lx"], spec["ly"], spec["jitter"], spec["seed"])
+    sv = Solver(dm, spec["order"], spec["equation"], _ffi.FLUX_LLF, _ffi.FP32, 1.4)
+    sv.project(spec["ic"], spec["params"])
+    sv.set_dt(None, cfl=0.7)
+    return sv
+
+
+def run_batched(steps: int = 20):
+    """Batched configuration: 256 independent solves advanced by the batched
+    graph step, against the same solves stepped one by one on the plain path."""
+    import torch
+    from dgcuda_gb300.batch import Batch
+    specs = _config4_requests(12349, 256, 16, 512)
+    solvers = [_native_solver(sp) for sp in specs]
+    dofs = sum(sv.nv * sv.np * sv.E for sv in solvers)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            for sv in solvers:
+                sv.step(sh)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            for sv in solvers:
+                sv.step(sh)
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = a.elapsed_time(b) / steps
+        bt = Batch(solvers)
+        bt.autotune(reps=2, stream=sh)
+        for _ in range(3):
+            bt.step(sh)
+        torch.cuda.synchronize()
+        l0 = bt.launch_count()
+        a.record(stream)
+        for _ in range(steps):
+            bt.step(sh)
+        b.record(stream)
+        torch.cuda.synchronize()
+        batch_ms = a.elapsed_time(b) / steps
+        launches = bt.launch_count() - l0
+        info = bt.info()
+        opts = bt.class_options()
+    bt.close()
+    for sv in solvers:
+        sv.close()
+    return {"workload": "256 solves: equation 50/50, N log-uniform [16,512] (2N^2 triangles), "
+                        "p uniform 1..4, Gaussian pulses / isentropic vortices, FP32, CFL 0.7",
+            "dofs_per_step": dofs, "elements": int(sum(2 * sp["n"] ** 2 for sp in specs)),
+            "value": dofs / (batch_ms * 1e-3), "ms_per_step": batch_ms,
+            "plain_value": dofs / (plain_ms * 1e-3), "plain_ms_per_step": plain_ms,
+            "speedup_vs_plain": plain_ms / batch_ms, "classes": info["classes"],
+            "work_items": info["items"], "launches_per_step": launches / steps,
+            "tuned_options": opts, "unit": UNIT}
+
+
+def run_served(rates=(50, 200, 1000, 2000), count: int = 400):
+    """Served configuration, scaled so every rate finishes in seconds: Poisson
+    arrivals of `count` requests per rate, sizes N log-uniform in [16,64],
+    orders 1..4, equations 50/50, end times U[0.1,1] x 0.02 flow-through times
+    (the stated configuration's N up to 512 and full flow-through end times
+    need hours per rate).  Also runs the same requests one by one on the plain
+    path for the throughput comparison."""
+    from dgcuda_gb300.serve import Server, request
+    out = []
+    rng = np.random.default_rng(12350)
+    plain = None
+    for ri, rate in enumerate(rates):
+        specs = _config4_requests(12350 + ri, count, 16, 64)
+        for sp in specs:
+            flow = sp["lx"] / 1.0            # flow-through time of the domain (unit speed)
+            sp["t_end"] = flow * rng.uniform(0.1, 1.0) * 0.02
+        srv = Server(budget_bytes=150 << 30, max_active=1024)
+        srv.set_steps_per_check(4)
+        gaps = rng.exponential(1.0 / rate, size=count)
+        t0 = time.perf_counter()
+        t_next = t0
+        for sp, g in zip(specs, gaps):
+            t_next += g
+            while time.perf_counter() < t_next:
+                pass
+            srv.submit(request(**sp))
+        srv.wait_idle(600.0)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        out.append({"rate_req_s": rate, "requests": count, "completed": st["completed"],
+                    "failed": st["failed"], "p50_s": st["p50_latency_s"],
+                    "p99_s": st["p99_latency_s"], "dof_updates": st["dof_updates"],
+                    "value": st["dof_updates"] / wall, "wall_s": wall, "repacks": st["repacks"]})
+        if plain is None:
+            # the same requests one by one on the plain path
+            import torch
+            tp0 = time.perf_counter()
+            dof = 0.0
+            for sp in specs:
+                sv = _native_solver(sp)
+                n, _ = sv.run(t_end=sp["t_end"])
+                dof += n * sv.nv * sv.np * sv.E
+                sv.close()
+            torch.cuda.synchronize()
+            plain = dof / (time.perf_counter() - tp0)
+    return {"workload": "Poisson arrivals, N log-uniform [16,64], p 1..4, equations 50/50, "
+                        "end times U[0.1,1] x 0.02 flow-through, 150 GB admission budget",
+            "rates": out, "plain_value": plain, "unit": UNIT}
+
+
 def run_ours(args, rank, world, local):
     import torch
     torch.cuda.set_device(local)
@@ -298,6 +434,9 @@ def run_ours(args, rank, world, local):
     }
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_sample()
+    if not args.no_extra:
+        out["batched"] = run_batched()
+        out["served"] = run_served()
     return out
 
 
@@ -309,6 +448,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mesh-n", type=int, default=1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched and served sections")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -37,6 +37,26 @@ class SolverDesc(C.Structure):
                 ("ax", C.c_double), ("ay", C.c_double)]
 
 
+class Request(C.Structure):
+    _fields_ = [("n", C.c_int), ("lx", C.c_double), ("ly", C.c_double), ("jitter", C.c_double),
+                ("seed", C.c_ulonglong), ("order", C.c_int), ("equation", C.c_int),
+                ("flux", C.c_int), ("precision", C.c_int), ("gamma", C.c_double),
+                ("ax", C.c_double), ("ay", C.c_double), ("ic", C.c_int),
+                ("params", C.c_double * 8), ("t_end", C.c_double), ("cfl", C.c_double),
+                ("dt", C.c_double), ("keep_state", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("failed", C.c_longlong),
+                ("active", C.c_longlong), ("queued", C.c_longlong), ("repacks", C.c_longlong),
+                ("steps", C.c_longlong), ("dof_updates", C.c_double),
+                ("busy_seconds", C.c_double), ("p50_latency_s", C.c_double),
+                ("p99_latency_s", C.c_double), ("max_latency_s", C.c_double),
+                ("device_bytes_in_use", C.c_size_t)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = 0, 1, 2, 3, 4
+
 # name -> (restype, argtypes); restype None means int status
 _vp, _dp, _ip, _i, _d, _sz = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int, C.c_double, C.c_size_t
 SIGNATURES = {
@@ -46,6 +66,8 @@ SIGNATURES = {
     "dgx_tables": (None, [_i, _ip] + [_dp] * 10),
     "dgx_mesh_create": (None, [_i, _i] + [_dp] * 6 + [_ip] * 7 + [C.POINTER(_vp)]),
     "dgx_mesh_destroy": (None, [_vp]),
+    "dgx_periodic_square_arrays": (None, [_i, _d, _d, _d, _d, _d, C.c_ulonglong, _dp, _ip, _ip]),
+    "dgx_mesh_create_periodic_square": (None, [_i, _d, _d, _d, _d, _d, C.c_ulonglong, C.POINTER(_vp)]),
     "dgx_mesh_geometry": (None, [_vp] + [_dp] * 9),
     "dgx_mesh_min_diameter": (None, [_vp, _dp]),
     "dgx_mesh_info": (None, [_vp, _ip, _ip, _ip]),
@@ -79,6 +101,19 @@ SIGNATURES = {
     "dgx_batch_info": (None, [_vp, _ip, _ip, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "dgx_batch_class_options": (None, [_vp, _i, _ip, _ip, _ip, _ip]),
     "dgx_batch_launch_count": (None, [_vp, C.POINTER(C.c_longlong)]),
+    "dgx_batch_progress": (None, [_vp, _dp, _dp, C.POINTER(C.c_uint), C.POINTER(C.c_longlong), _vp]),
+    "dgx_batch_set_options": (None, [_vp, _i, _i, _i]),
+    "dgx_server_create": (None, [_sz, _i, C.POINTER(_vp)]),
+    "dgx_server_submit": (None, [_vp, C.POINTER(Request), C.POINTER(C.c_longlong)]),
+    "dgx_server_status": (None, [_vp, C.c_longlong, _ip, _dp]),
+    "dgx_server_result": (None, [_vp, C.c_longlong, _dp, _sz, _dp, _ip, _dp]),
+    "dgx_server_cancel": (None, [_vp, C.c_longlong]),
+    "dgx_server_release": (None, [_vp, C.c_longlong]),
+    "dgx_server_wait_idle": (None, [_vp, _d]),
+    "dgx_server_get_stats": (None, [_vp, C.POINTER(ServerStats)]),
+    "dgx_server_set_steps_per_check": (None, [_vp, _i]),
+    "dgx_server_inject_stall": (None, [_vp, _d]),
+    "dgx_server_destroy": (None, [_vp]),
 }
 
 _lib = None

@@ -52,6 +52,11 @@ using namespace dgx;
 
 struct dgx_batch {
     std::vector<dgx_solver *> solvers;
+    const double **d_scal = nullptr;        // each solve's device scalars
+    const unsigned int **d_status = nullptr;
+    const long long **d_steps = nullptr;
+    double *d_progress = nullptr;          // [n][4]: t, dt, status, steps
+    double *h_progress = nullptr;          // pinned copy
     std::vector<BatchClass> classes;
     DtArgs *d_dt = nullptr;
     int2 *d_cfl_items = nullptr;
@@ -170,8 +175,23 @@ int build_graph(dgx_batch *b) {
     return DGX_OK;
 }
 
+__global__ void progress_kernel(const double *const *scal, const unsigned int *const *status,
+                                const long long *const *steps, int n, double *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[4 * i] = scal[i][1];
+    out[4 * i + 1] = scal[i][0];
+    out[4 * i + 2] = static_cast<double>(*status[i]);
+    out[4 * i + 3] = static_cast<double>(*steps[i]);
+}
+
 void batch_free(dgx_batch *b) {
     destroy_graph(b);
+    if (b->d_scal) cudaFree(b->d_scal);
+    if (b->d_status) cudaFree(b->d_status);
+    if (b->d_steps) cudaFree(b->d_steps);
+    if (b->d_progress) cudaFree(b->d_progress);
+    if (b->h_progress) cudaFreeHost(b->h_progress);
     for (auto &k : b->classes) {
         for (auto p : k.d_args)
             if (p) cudaFree(p);
@@ -227,6 +247,28 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
         for (int blk = 0; blk < dts[i].nblocks; ++blk) cfl_items.push_back(make_int2(i, blk));
     }
     b->n_cfl_items = static_cast<int>(cfl_items.size());
+    {
+        std::vector<const double *> sc(n);
+        std::vector<const unsigned int *> stt(n);
+        std::vector<const long long *> stp(n);
+        for (int i = 0; i < n; ++i) {
+            sc[i] = solvers[i]->s.scal;
+            stt[i] = solvers[i]->s.status;
+            stp[i] = solvers[i]->s.steps;
+        }
+        if (cudaMalloc(&b->d_scal, sizeof(double *) * n) != cudaSuccess ||
+            cudaMalloc(&b->d_status, sizeof(unsigned int *) * n) != cudaSuccess ||
+            cudaMalloc(&b->d_steps, sizeof(long long *) * n) != cudaSuccess ||
+            cudaMalloc(&b->d_progress, sizeof(double) * 4 * n) != cudaSuccess ||
+            cudaMallocHost(&b->h_progress, sizeof(double) * 4 * n) != cudaSuccess ||
+            cudaMemcpy(b->d_steps, stp.data(), sizeof(long long *) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(b->d_scal, sc.data(), sizeof(double *) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(b->d_status, stt.data(), sizeof(unsigned int *) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+            set_error("batch progress buffers failed");
+            batch_free(b);
+            return DGX_ERR_NOMEM;
+        }
+    }
     if (cudaMalloc(&b->d_dt, sizeof(DtArgs) * n) != cudaSuccess ||
         cudaMalloc(&b->d_cfl_items, sizeof(int2) * cfl_items.size()) != cudaSuccess) {
         set_error("cudaMalloc failed");
@@ -316,6 +358,34 @@ int dgx_batch_class_options(const dgx_batch *b, int cls, int *order, int *equati
     if (prefetch) *prefetch = k.prefetch;
     if (persistent) *persistent = k.persistent;
     return DGX_OK;
+}
+
+int dgx_batch_progress(dgx_batch *b, double *t, double *dt, unsigned int *status, long long *steps,
+                       void *stream) {
+    if (!b) return DGX_ERR_INVALID;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int n = static_cast<int>(b->solvers.size());
+    progress_kernel<<<(n + 127) / 128, 128, 0, st>>>(b->d_scal, b->d_status, b->d_steps, n, b->d_progress);
+    DGX_CHECK_LAUNCH();
+    DGX_TRY_CUDA(cudaMemcpyAsync(b->h_progress, b->d_progress, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st));
+    DGX_TRY_CUDA(cudaStreamSynchronize(st));
+    for (int i = 0; i < n; ++i) {
+        if (t) t[i] = b->h_progress[4 * i];
+        if (dt) dt[i] = b->h_progress[4 * i + 1];
+        if (status) status[i] = static_cast<unsigned int>(b->h_progress[4 * i + 2]);
+        if (steps) steps[i] = static_cast<long long>(b->h_progress[4 * i + 3]);
+    }
+    return DGX_OK;
+}
+
+int dgx_batch_set_options(dgx_batch *b, int cls, int prefetch, int persistent) {
+    if (!b || cls < 0 || cls >= static_cast<int>(b->classes.size())) return DGX_ERR_INVALID;
+    auto &k = b->classes[cls];
+    k.prefetch = prefetch ? 1 : 0;
+    k.persistent = persistent < 0 ? 0 : persistent;
+    int rc = class_upload(b, k);
+    if (!rc) rc = build_graph(b);
+    return rc;
 }
 
 int dgx_batch_launch_count(const dgx_batch *b, long long *count) {

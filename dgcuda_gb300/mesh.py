@@ -22,7 +22,25 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-__all__ = ["Mesh", "periodic_square", "scramble", "dirichlet_square"]
+__all__ = ["Mesh", "periodic_square", "scramble", "dirichlet_square", "unit_draws"]
+
+
+def _splitmix64(x: np.ndarray) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        x = x + np.uint64(0x9E3779B97F4A7C15)
+        x = (x ^ (x >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        x = (x ^ (x >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return x ^ (x >> np.uint64(31))
+
+
+def unit_draws(seed: int, k: np.ndarray) -> np.ndarray:
+    """Uniform [0,1) draws of a counter-based generator: draw k of stream `seed`
+    is splitmix64(seed * golden + k) >> 11, scaled by 2^-53.  The native mesh
+    generator (dgx_meshgen.cpp) uses the same draws."""
+    with np.errstate(over="ignore"):
+        base = np.array([seed], dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15)
+        v = _splitmix64(base + np.asarray(k, dtype=np.uint64))
+    return (v >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
 
 
 @dataclass
@@ -103,8 +121,10 @@ def periodic_square(n: int, lx: float = 1.0, ly: float = 1.0, x0: float = 0.0,
     ``n x n`` squares, each split along its SW-NE diagonal into a lower
     triangle (SW, SE, NE) and an upper triangle (SW, NE, NW): ``2 n^2``
     elements and ``3 n^2`` sides.  Interior vertices move by independent
-    uniform offsets in ``[-jitter h, +jitter h]`` (seeded); boundary vertices
-    stay put so that periodic images coincide.  Element ``2q`` and ``2q+1``
+    uniform offsets ``jitter h (2u - 1)`` (u from :func:`unit_draws` of the
+    seed and the vertex index j*(n+1)+i); boundary vertices stay put so that
+    periodic images coincide.  Bit-identical to the native generator
+    ``dgx_periodic_square_arrays``.  Element ``2q`` and ``2q+1``
     belong to square ``q = j n + i``; sides ``3q``, ``3q+1``, ``3q+2`` are its
     bottom, left and diagonal sides, so neighbouring elements have nearby
     indices.
@@ -116,9 +136,9 @@ def periodic_square(n: int, lx: float = 1.0, ly: float = 1.0, x0: float = 0.0,
     X = x0 + ii * hx
     Y = y0 + jj * hy
     if jitter > 0 and n > 1:
-        rng = np.random.default_rng(seed)
-        dx = rng.uniform(-jitter * hx, jitter * hx, size=(n - 1, n - 1))
-        dy = rng.uniform(-jitter * hy, jitter * hy, size=(n - 1, n - 1))
+        v = (jj[1:n, 1:n] * (n + 1) + ii[1:n, 1:n]).astype(np.uint64)
+        dx = (jitter * hx) * (2.0 * unit_draws(seed, 2 * v) - 1.0)
+        dy = (jitter * hy) * (2.0 * unit_draws(seed, 2 * v + 1) - 1.0)
         X = X.copy(); Y = Y.copy()
         X[1:n, 1:n] += dx
         Y[1:n, 1:n] += dy

@@ -51,13 +51,26 @@ class DeviceMesh:
         call("dgx_mesh_create", mesh.num_elem, mesh.num_sides, *[_dp(a) for a in V],
              *[_ip(a) for a in I], C.byref(h))
         self.h = h
+        self.num_elem = mesh.num_elem
+        self.num_sides = mesh.num_sides
 
-    @property
-    def num_elem(self):
-        return self.mesh.num_elem
+    @classmethod
+    def periodic_square(cls, n: int, lx: float = 1.0, ly: float = 1.0, jitter: float = 0.0,
+                        seed: int = 0) -> "DeviceMesh":
+        """A structured periodic mesh built by the native generator (identical
+        to dgcuda_gb300.mesh.periodic_square with the same arguments)."""
+        self = cls.__new__(cls)
+        self.mesh = None
+        h = C.c_void_p()
+        call("dgx_mesh_create_periodic_square", int(n), float(lx), float(ly), 0.0, 0.0,
+             float(jitter), int(seed), C.byref(h))
+        self.h = h
+        self.num_elem = 2 * n * n
+        self.num_sides = 3 * n * n
+        return self
 
     def geometry(self) -> dict:
-        E, S = self.mesh.num_elem, self.mesh.num_sides
+        E, S = self.num_elem, self.num_sides
         out = {k: np.zeros(E) for k in ("J", "xr", "yr", "xs", "ys", "diam")}
         out.update({k: np.zeros(S) for k in ("len", "nx", "ny")})
         call("dgx_mesh_geometry", self.h, *[_dp(out[k]) for k in

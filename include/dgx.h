@@ -104,6 +104,17 @@ int dgx_mesh_create(int num_elem, int num_sides, const double *V1x, const double
                     const int *elem_s3, const int *left_elem, const int *right_elem,
                     const int *left_side_number, const int *right_side_number,
                     dgx_mesh **out);
+/* Structured periodic triangulation of [x0,x0+lx] x [y0,y0+ly]: n x n squares
+ * split along their SW-NE diagonal (2n^2 elements, 3n^2 sides), interior
+ * vertices jittered by jitter*h*(2u-1) with u from a counter-based generator
+ * of `seed`.  The synthetic meshes of the benchmark configurations (the
+ * reference reads its meshes from .pmsh files, conserv.cu:118-192).
+ * dgx_periodic_square_arrays fills host arrays V[6][E], elem_s[3][E],
+ * sides[4][S] (left_elem, right_elem, left_side, right_side) without a GPU. */
+int dgx_periodic_square_arrays(int n, double lx, double ly, double x0, double y0, double jitter,
+                               unsigned long long seed, double *V, int *elem_s, int *sides);
+int dgx_mesh_create_periodic_square(int n, double lx, double ly, double x0, double y0,
+                                    double jitter, unsigned long long seed, dgx_mesh **out);
 int dgx_mesh_destroy(dgx_mesh *mesh);
 /* FP64 geometric factors copied to host arrays (NULL to skip): J, x_r, y_r,
  * x_s, y_s, inscribed diameter per element; length, Nx, Ny per side. */
@@ -215,6 +226,66 @@ int dgx_batch_info(const dgx_batch *batch, int *num_classes, int *num_items, lon
 int dgx_batch_class_options(const dgx_batch *batch, int cls, int *order, int *equation,
                             int *prefetch, int *persistent);
 int dgx_batch_launch_count(const dgx_batch *batch, long long *count);
+/* Per solve (in creation order): current time, last dt, status flags
+ * (nonzero: non-finite or unphysical state) and completed steps, gathered in
+ * one copy; any output may be NULL; synchronous. */
+int dgx_batch_progress(dgx_batch *batch, double *t, double *dt, unsigned int *status,
+                       long long *steps, void *stream);
+/* Set the kernel options of one class by hand and rebuild the graph. */
+int dgx_batch_set_options(dgx_batch *batch, int cls, int prefetch, int persistent);
+
+/* --- serving: continuous batching of solve requests ------------------------ */
+/* New, no counterpart in the reference.  A worker thread admits queued requests
+ * while the device-memory budget and slot count allow, keeps their state on the
+ * device, repacks the running set into a batch whenever solves join or finish,
+ * advances it a few steps at a time and retires finished solves, recording
+ * time-to-solution.  A request's result is the same alone and in the mix. */
+typedef struct dgx_server dgx_server;
+typedef struct dgx_request {
+    int n;                       /* periodic square mesh: n x n squares ...            */
+    double lx, ly, jitter;       /* ... of [0,lx] x [0,ly], jitter (dgx_mesh_create_periodic_square) */
+    unsigned long long seed;     /* equal mesh specs share one device mesh              */
+    int order, equation, flux, precision;
+    double gamma, ax, ay;
+    int ic;                      /* dgx_ic with params                                  */
+    double params[8];
+    double t_end;                /* end time (the last step is clipped to it)           */
+    double cfl;                  /* CFL factor when dt <= 0                             */
+    double dt;                   /* > 0: fixed time step                                */
+    int keep_state;              /* keep the final state for dgx_server_result          */
+} dgx_request;
+enum dgx_request_state { DGX_REQ_QUEUED = 0, DGX_REQ_RUNNING = 1, DGX_REQ_DONE = 2,
+                         DGX_REQ_FAILED = 3, DGX_REQ_CANCELLED = 4 };
+typedef struct dgx_server_stats {
+    long long submitted, completed, failed, active, queued, repacks, steps;
+    double dof_updates;          /* DOF-updates performed by completed and running solves */
+    double busy_seconds;         /* worker time spent stepping                          */
+    double p50_latency_s, p99_latency_s, max_latency_s;   /* time-to-solution           */
+    size_t device_bytes_in_use;  /* admitted footprint                                  */
+} dgx_server_stats;
+/* budget_bytes: admission limit on the estimated device footprint of running
+ * requests; max_active: slot limit. */
+int dgx_server_create(size_t budget_bytes, int max_active, dgx_server **out);
+/* Queue a request (validated here: DGX_ERR_INVALID / DGX_ERR_UNSUPPORTED; a
+ * request larger than the whole budget: DGX_ERR_BUSY). */
+int dgx_server_submit(dgx_server *server, const dgx_request *request, long long *id);
+/* state (dgx_request_state) and time-to-solution once finished (else -1) */
+int dgx_server_status(dgx_server *server, long long id, int *state, double *latency_s);
+/* Result of a finished request: final state (if kept, c_len >= its size),
+ * conserved totals (4 doubles), steps and final time; any output may be NULL. */
+int dgx_server_result(dgx_server *server, long long id, double *c, size_t c_len, double *totals,
+                      int *steps, double *t_final);
+int dgx_server_cancel(dgx_server *server, long long id);
+/* forget a finished, failed or cancelled request */
+int dgx_server_release(dgx_server *server, long long id);
+/* wait until nothing is queued or running; DGX_ERR_TIMEOUT after timeout_s */
+int dgx_server_wait_idle(dgx_server *server, double timeout_s);
+int dgx_server_get_stats(dgx_server *server, dgx_server_stats *out);
+/* steps advanced between two completion checks (default 8) */
+int dgx_server_set_steps_per_check(dgx_server *server, int steps);
+/* Fault injection on the host: the worker sleeps `seconds` after every check. */
+int dgx_server_inject_stall(dgx_server *server, double seconds);
+int dgx_server_destroy(dgx_server *server);
 
 #ifdef __cplusplus
 }

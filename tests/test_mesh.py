@@ -36,3 +36,20 @@ def test_scramble_keeps_mesh_valid():
         s = scramble(m, seed=seed)
         s.check()
         assert abs(s.jacobian().sum() - m.jacobian().sum()) < 1e-12
+
+
+@pytest.mark.parametrize("n,jit,seed", [(1, 0.0, 0), (5, 0.15, 12347), (16, 0.3, 7)])
+def test_native_generator_matches_python(n, jit, seed, native):
+    import ctypes as C
+    from dgcuda_gb300 import _ffi
+    m = periodic_square(n, lx=2.0, ly=3.0, x0=-1.0, y0=0.5, jitter=jit, seed=seed)
+    E, S = m.num_elem, m.num_sides
+    V = np.zeros(6 * E)
+    es = np.zeros(3 * E, dtype=np.int32)
+    sd = np.zeros(4 * S, dtype=np.int32)
+    _ffi.call("dgx_periodic_square_arrays", n, 2.0, 3.0, -1.0, 0.5, jit, seed,
+              V.ctypes.data_as(C.POINTER(C.c_double)), es.ctypes.data_as(C.POINTER(C.c_int)),
+              sd.ctypes.data_as(C.POINTER(C.c_int)))
+    np.testing.assert_array_equal(V.reshape(6, E), np.stack(m.vertices()))
+    np.testing.assert_array_equal(es.reshape(3, E), np.stack(m.elem_sides()))
+    np.testing.assert_array_equal(sd.reshape(4, S), np.stack(m.side_arrays()))
