@@ -228,6 +228,41 @@ def _native_solver(spec):
     return sv
 
 
+def run_accuracy(mesh_n: int, steps: int = 100):
+    """Config-3 accuracy: the FP32 path and the FP64 path on the same mesh and
+    initial state for `steps` RK4 steps with the same fixed dt (the FP32 run's
+    first CFL dt); relative L2 per conserved variable of FP32 against FP64, and
+    the FP32 run's drift of the conserved totals (FP64 reductions).  The FP64
+    path stands in for the FP64 oracle at this size: tests/test_gpu_parity.py
+    holds it to 1e-11 of the CPU oracle on smaller meshes."""
+    from dgcuda_gb300 import _ffi
+    from dgcuda_gb300.solver import DeviceMesh, Solver
+    dm = DeviceMesh.periodic_square(mesh_n, 1.0, 1.0, 0.15, 12347)
+    res = {}
+    for prec in (_ffi.FP32, _ffi.FP64):
+        sv = Solver(dm, 3, _ffi.EULER, _ffi.FLUX_LLF, prec, 1.4)
+        sv.project(_ffi.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
+        res[prec] = sv
+    s32, s64 = res[_ffi.FP32], res[_ffi.FP64]
+    s32.set_dt(None)
+    s32.run(max_steps=1)
+    _, dt = s32.time()
+    s32.project(_ffi.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
+    s32.reset_time(0.0)
+    t0 = s32.totals()
+    for sv in (s32, s64):
+        sv.set_dt(dt)
+        sv.run(max_steps=steps)
+    c32, c64 = s32.get_state(), s64.get_state()
+    t1 = s32.totals()
+    nv = c32.shape[0]
+    err = [float(np.linalg.norm(c32[n] - c64[n]) / np.linalg.norm(c64[n])) for n in range(nv)]
+    drift = [float(abs(t1[n] - t0[n]) / max(abs(t0[n]), abs(t0[0]))) for n in range(nv)]
+    return {"steps": steps, "dt": dt, "rel_l2_fp32_vs_fp64": err, "conserved_total_drift_fp32": drift,
+            "max_rel_l2": max(err), "meets_1e-5": max(err) <= 1e-5,
+            "reference": "FP64 path on the GPU (held to 1e-11 of the FP64 CPU oracle in the parity tests)"}
+
+
 def run_batched(steps: int = 20):
     """Batched configuration: 256 independent solves advanced by the batched
     graph step, against the same solves stepped one by one on the plain path."""
@@ -435,6 +470,7 @@ def run_ours(args, rank, world, local):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_sample()
     if not args.no_extra:
+        out["accuracy"] = run_accuracy(args.mesh_n)
         out["batched"] = run_batched()
         out["served"] = run_served()
     return out

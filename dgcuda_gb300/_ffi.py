@@ -66,6 +66,11 @@ SIGNATURES = {
     "dgx_tables": (None, [_i, _ip] + [_dp] * 10),
     "dgx_mesh_create": (None, [_i, _i] + [_dp] * 6 + [_ip] * 7 + [C.POINTER(_vp)]),
     "dgx_mesh_destroy": (None, [_vp]),
+    "dgx_pmsh_info": (None, [C.c_char_p, _ip, _ip]),
+    "dgx_pmsh_read": (None, [C.c_char_p, _dp, _ip, _ip]),
+    "dgx_pmsh_write": (None, [C.c_char_p, _i, _i, _dp, _ip, _ip]),
+    "dgx_mesh_create_from_pmsh": (None, [C.c_char_p, C.POINTER(_vp)]),
+    "dgx_write_vertex_values": (None, [_vp, C.c_char_p]),
     "dgx_periodic_square_arrays": (None, [_i, _d, _d, _d, _d, _d, C.c_ulonglong, _dp, _ip, _ip]),
     "dgx_mesh_create_periodic_square": (None, [_i, _d, _d, _d, _d, _d, C.c_ulonglong, C.POINTER(_vp)]),
     "dgx_mesh_geometry": (None, [_vp] + [_dp] * 9),

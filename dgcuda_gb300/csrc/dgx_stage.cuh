@@ -31,9 +31,26 @@
 #error "define DGX_REAL before including dgx_stage.cuh"
 #endif
 
+// Loops over quadrature points (and, optionally, sides) are kept rolled: the
+// fully unrolled kernel is several times larger than the instruction cache and
+// stalls on instruction fetch; with a uniform loop index the table operands
+// still come from the constant bank.
+#ifndef DGX_ROLLED_VOLUME
+#define DGX_ROLLED_VOLUME 1
+#endif
+#ifndef DGX_ROLLED_SIDES
+#define DGX_ROLLED_SIDES 0
+#endif
+#ifndef DGX_ROLLED_TRACES
+#define DGX_ROLLED_TRACES 1
+#endif
+
 namespace dgx {
 
 static __constant__ DGX_REAL c_tab[kTableTotal];
+
+template <typename T>
+__device__ __forceinline__ T pick3(T a0, T a1, T a2, int k) { return k == 0 ? a0 : (k == 1 ? a1 : a2); }
 
 template <int P>
 struct Lay {
@@ -144,10 +161,13 @@ __device__ __forceinline__ void num_flux(const R *UL, const R *UR, R nx, R ny, i
 }
 
 // Shared memory of one CTA: the side tables (for traces on a runtime side) and
-// the trace slots, stored value-major: s_tr[(j*NV + n) * nslot + slot], so that
-// threads reading their own slots 3*tid + k hit distinct banks.
+// the trace slots, slot-major with an odd stride: s_tr[slot * TSW + j*NV + n],
+// so a thread addresses a whole slot from one base register and threads
+// reading their own slots 3*tid + k (stride 3*TSW, odd) hit distinct banks.
 template <int P, int NV>
 DGX_HD constexpr int side_table_words() { return (3 * num_modes(P) * num_quad1(P) + 3) & ~3; }
+template <int P, int NV>
+DGX_HD constexpr int slot_words() { return (NV * num_quad1(P)) | 1; }
 
 // bytes of the prefetched epilogue operands (base state and accumulator slices
 // of the tile: 2 x NV x NP planes of kTile values)
@@ -159,7 +179,7 @@ DGX_HD constexpr size_t prefetch_bytes() {
 template <int P, int NV>
 DGX_HD constexpr size_t stage_smem_bytes(int nslot, int prefetch) {
     return 16 + sizeof(R) * (static_cast<size_t>(side_table_words<P, NV>()) +
-                             static_cast<size_t>(NV) * num_quad1(P) * nslot) +
+                             static_cast<size_t>(slot_words<P, NV>()) * nslot) +
            (prefetch ? prefetch_bytes<P, NV>() : 0);
 }
 
@@ -180,7 +200,8 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
     // epilogue operands (base state, accumulator) of the tile, prefetched by the
     // TMA engine while the element work runs; 16-byte aligned (side_table_words
     // is a multiple of 4 and nslot of kTile-sized planes keeps alignment)
-    R *s_pre = s_tr + static_cast<size_t>(NV) * NQ1 * nslot;
+    constexpr int TSW = slot_words<P, NV>();
+    R *s_pre = s_tr + static_cast<size_t>(TSW) * nslot;
 
     R dt;
     if (a.mode == 0) {
@@ -261,8 +282,12 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
             for (int i = 0; i < NP; ++i) cn[n][i] = __ldg(u + (n * NP + i) * SE + ne);
     }
 
-    // own traces on the three sides (compile-time side tables)
+    // own traces on the three sides (constant-bank side tables)
+#if DGX_ROLLED_TRACES
+#pragma unroll 1
+#else
 #pragma unroll
+#endif
     for (int k = 0; k < 3; ++k)
 #pragma unroll
         for (int j = 0; j < NQ1; ++j)
@@ -271,7 +296,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
                 R s = R(0);
 #pragma unroll
                 for (int i = 0; i < NP; ++i) s = fma(c[n][i], c_tab[L::SIDE + (k * NP + i) * NQ1 + j], s);
-                s_tr[(j * NV + n) * nslot + 3 * tid + k] = s;
+                s_tr[(3 * tid + k) * TSW + j * NV + n] = s;
             }
     __syncthreads();   // s_side ready
 
@@ -303,7 +328,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
 #pragma unroll
         for (int j = 0; j < NQ1; ++j)
 #pragma unroll
-            for (int n = 0; n < NV; ++n) s_tr[(j * NV + n) * nslot + 3 * kTile + h] = tr[j][n];
+            for (int n = 0; n < NV; ++n) s_tr[(3 * kTile + h) * TSW + j * NV + n] = tr[j][n];
     }
 
     R rhs[NV][NP];
@@ -319,7 +344,11 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
         const R xr = __ldg(geo + SE + e), yr = __ldg(geo + 2 * SE + e);
         const R xs = __ldg(geo + 3 * SE + e), ys = __ldg(geo + 4 * SE + e);
         // ---- volume integral ----------------------------------------------------
+#if DGX_ROLLED_VOLUME
+#pragma unroll 1
+#else
 #pragma unroll
+#endif
         for (int q = 0; q < NQ; ++q) {
             R U[NV], fx[NV], fy[NV];
 #pragma unroll
@@ -347,22 +376,29 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
     }
 
     // ---- the three sides --------------------------------------------------------
+#if DGX_ROLLED_SIDES
+#pragma unroll 1
+#else
 #pragma unroll
+#endif
     for (int k = 0; k < 3; ++k) {
-        const int word = sw[k];
-        const R nx = snx[k], ny = sny[k], hl = shl[k];
+        const int word = pick3(sw[0], sw[1], sw[2], k);
+        const R nx = pick3(snx[0], snx[1], snx[2], k), ny = pick3(sny[0], sny[1], sny[2], k);
+        const R hl = pick3(shl[0], shl[1], shl[2], k);
         const int own = 3 * tid + k;
         // a boundary side (rejected at solver creation) would mirror the own trace
         const int slot = word >= 0 ? (word >> 1) : own;
         const int il = word >= 0 ? (word & 1) : 1;
+        const R *s_own = s_tr + own * TSW;
+        const R *s_nbr = s_tr + slot * TSW;
         R Fh[NQ1][NV];
 #pragma unroll
         for (int j = 0; j < NQ1; ++j) {
             R UO[NV], UN[NV], UL[NV], UR[NV];
 #pragma unroll
             for (int n = 0; n < NV; ++n) {
-                UO[n] = s_tr[(j * NV + n) * nslot + own];
-                UN[n] = s_tr[((NQ1 - 1 - j) * NV + n) * nslot + slot];
+                UO[n] = s_own[j * NV + n];
+                UN[n] = s_nbr[(NQ1 - 1 - j) * NV + n];
                 UL[n] = il ? UO[n] : UN[n];
                 UR[n] = il ? UN[n] : UO[n];
             }
@@ -450,8 +486,11 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
     return pre;
 }
 
+#ifndef DGX_MIN_CTAS_P3
+#define DGX_MIN_CTAS_P3 3
+#endif
 template <int P>
-constexpr int min_ctas() { return P <= 3 ? 4 : 2; }
+constexpr int min_ctas() { return P <= 3 ? DGX_MIN_CTAS_P3 : 2; }
 
 // Plain path: one CTA per tile of one solve.
 template <int P, int EQ>
@@ -470,11 +509,18 @@ __global__ void __launch_bounds__(kTile, min_ctas<P>()) batch_stage_kernel(const
     extern __shared__ __align__(16) unsigned char smem_raw[];
     if (threadIdx.x == 0) mbar_init(reinterpret_cast<unsigned long long *>(smem_raw), 1);
     __syncthreads();
+    // the item's solve arguments live in shared memory, not registers
+    __shared__ StageArgs s_args;
     unsigned phase = 0;
     for (int it = blockIdx.x; it < b.n_items; it += gridDim.x) {
         const int2 w = b.items[it];
-        const StageArgs a = b.args[w.x];
-        if (stage_tile<P, EQ>(a, w.y, smem_raw, phase & 1u)) ++phase;
+        constexpr int kWords = sizeof(StageArgs) / sizeof(int);
+        static_assert(sizeof(StageArgs) % sizeof(int) == 0, "StageArgs is copied word by word");
+        if (threadIdx.x < kWords)
+            reinterpret_cast<int *>(&s_args)[threadIdx.x] =
+                reinterpret_cast<const int *>(b.args + w.x)[threadIdx.x];
+        __syncthreads();
+        if (stage_tile<P, EQ>(s_args, w.y, smem_raw, phase & 1u)) ++phase;
         __syncthreads();   // shared memory is reused by the next item
     }
 }
@@ -489,12 +535,30 @@ static int launch_one(const StageArgs &a_in, cudaStream_t st) {
     if (smem > 48 * 1024 && smem > configured) {
         DGX_TRY_CUDA(cudaFuncSetAttribute(stage_kernel<P, EQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(smem)));
+        // all of the unified L1 / shared storage as shared memory, so that
+        // several CTAs with large tiles fit on an SM
+        DGX_TRY_CUDA(cudaFuncSetAttribute(stage_kernel<P, EQ>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                          100));
         configured = smem;
     }
     const int grid = (a.E + kTile - 1) / kTile;
     if (grid > 0) stage_kernel<P, EQ><<<grid, kTile, smem, st>>>(a);
     DGX_CHECK_LAUNCH();
     return DGX_OK;
+}
+
+// Batched path, one item per CTA (the flat grid): no loop to keep live state across.
+template <int P, int EQ>
+__global__ void __launch_bounds__(kTile, min_ctas<P>()) batch_stage_kernel_flat(const BatchStageArgs b) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ StageArgs s_args;
+    constexpr int kWords = sizeof(StageArgs) / sizeof(int);
+    const int2 w = b.items[blockIdx.x];
+    if (threadIdx.x == 0) mbar_init(reinterpret_cast<unsigned long long *>(smem_raw), 1);
+    if (threadIdx.x < kWords)
+        reinterpret_cast<int *>(&s_args)[threadIdx.x] = reinterpret_cast<const int *>(b.args + w.x)[threadIdx.x];
+    __syncthreads();
+    stage_tile<P, EQ>(s_args, w.y, smem_raw, 0u);
 }
 
 template <int P, int EQ>
@@ -505,9 +569,14 @@ static int launch_batch_one(const BatchStageArgs &b, cudaStream_t st) {
     if (smem > 48 * 1024 && smem > configured) {
         DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel<P, EQ>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel_flat<P, EQ>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel<P, EQ>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel_flat<P, EQ>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         configured = smem;
     }
-    if (b.grid > 0) batch_stage_kernel<P, EQ><<<b.grid, kTile, smem, st>>>(b);
+    if (b.grid > 0 && b.grid >= b.n_items) batch_stage_kernel_flat<P, EQ><<<b.n_items, kTile, smem, st>>>(b);
+    else if (b.grid > 0) batch_stage_kernel<P, EQ><<<b.grid, kTile, smem, st>>>(b);
     DGX_CHECK_LAUNCH();
     return DGX_OK;
 }

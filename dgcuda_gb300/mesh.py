@@ -22,7 +22,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-__all__ = ["Mesh", "periodic_square", "scramble", "dirichlet_square", "unit_draws"]
+__all__ = ["Mesh", "periodic_square", "scramble", "dirichlet_square", "unit_draws", "write_pmsh",
+           "read_pmsh", "read_gmsh"]
 
 
 def _splitmix64(x: np.ndarray) -> np.ndarray:
@@ -261,3 +262,106 @@ def scramble(m: Mesh, seed: int = 0, rotate: bool = True, swap: bool = True,
                meta=dict(m.meta, scrambled=seed))
     out.check()
     return out
+
+
+# ---------------------------------------------------------------------------
+# File formats
+# ---------------------------------------------------------------------------
+
+def write_pmsh(mesh: Mesh, path: str) -> None:
+    """Write the reference's .pmsh text format (src/2d/genmesh.py:290-308), with
+    full-precision coordinates; side end points are the left element's."""
+    E, S = mesh.num_elem, mesh.num_sides
+    V = np.stack(mesh.vertices())
+    es = np.stack(mesh.elem_sides())
+    P = V.reshape(3, 2, E)
+    with open(path, "w") as f:
+        f.write(f"{E}\n")
+        for e in range(E):
+            f.write(" ".join(repr(float(x)) for x in V[:, e]) + f" {es[0, e]} {es[1, e]} {es[2, e]}\n")
+        f.write(f"{S}\n")
+        for s in range(S):
+            L, ls = int(mesh.left_elem[s]), int(mesh.left_side[s])
+            a = [float(x) for x in P[ls, :, L]]
+            b = [float(x) for x in P[(ls + 1) % 3, :, L]]
+            f.write(f"{a[0]!r} {a[1]!r} {b[0]!r} {b[1]!r} {L} {int(mesh.right_elem[s])} {ls} "
+                    f"{int(mesh.right_side[s])}\n")
+
+
+def read_pmsh(path: str) -> Mesh:
+    """Read a .pmsh file (the reference's read_mesh, src/2d/conservation/conserv.cu:118-192)."""
+    with open(path) as f:
+        lines = [ln for ln in f.read().splitlines() if ln.strip()]
+    E = int(lines[0].split()[0])
+    el = np.array([ln.split()[:9] for ln in lines[1:1 + E]], dtype=np.float64)
+    S = int(lines[1 + E].split()[0])
+    sd = np.array([ln.split()[:8] for ln in lines[2 + E:2 + E + S]], dtype=np.float64)
+    return Mesh(*el[:, :6].T, *el[:, 6:9].T.astype(np.int64), *sd[:, 4:8].T.astype(np.int64),
+                meta=dict(kind="pmsh", path=path))
+
+
+BOUNDARY_TAGS = {10000: -1, 20000: -2, 30000: -3}   # physical tags of genmesh.py:170-180
+
+
+def read_gmsh(path_or_text: str, boundary_tags=None) -> Mesh:
+    """Gmsh v2.2 ASCII .msh -> Mesh, the job of the reference's Python-2
+    converter (src/2d/genmesh.py:11-310) restated for Python 3.  Triangles
+    become elements (clockwise ones are reordered to counter-clockwise);
+    sides are matched by their vertex pair, the first element to meet a side
+    is its left element; line elements tag boundary sides by their physical
+    group (10000 reflecting -> -1, 20000 outflow -> -2, 30000 inflow -> -3);
+    boundary sides are sorted first, in the order -1, -2, -3."""
+    tags = dict(BOUNDARY_TAGS if boundary_tags is None else boundary_tags)
+    text = path_or_text
+    if "\n" not in path_or_text:
+        with open(path_or_text) as f:
+            text = f.read()
+    lines = text.splitlines()
+    i = lines.index("$Nodes")
+    n_nodes = int(lines[i + 1])
+    node_id, xy = {}, []
+    for k in range(n_nodes):
+        parts = lines[i + 2 + k].split()
+        node_id[int(parts[0])] = k
+        xy.append((float(parts[1]), float(parts[2])))
+    xy = np.array(xy)
+    i = lines.index("$Elements")
+    n_el = int(lines[i + 1])
+    tris, bnd = [], {}
+    for k in range(n_el):
+        parts = [int(x) for x in lines[i + 2 + k].split()]
+        etype, ntags = parts[1], parts[2]
+        phys = parts[3] if ntags > 0 else 0
+        nodes = [node_id[x] for x in parts[3 + ntags:]]
+        if etype == 2:
+            a, b, c = nodes[:3]
+            J = (xy[b, 0] - xy[a, 0]) * (xy[c, 1] - xy[a, 1]) - (xy[c, 0] - xy[a, 0]) * (xy[b, 1] - xy[a, 1])
+            tris.append((a, c, b) if J < 0 else (a, b, c))
+        elif etype == 1:
+            bnd[frozenset(nodes[:2])] = tags.get(phys, -1)
+    E = len(tris)
+    es = np.zeros((E, 3), dtype=np.int64)
+    le, re, ls, rs = [], [], [], []
+    side_of = {}
+    for e, t in enumerate(tris):
+        for k in range(3):
+            key = frozenset((t[k], t[(k + 1) % 3]))
+            if key in side_of:
+                s = side_of[key]
+                re[s], rs[s] = e, k
+            else:
+                s = len(le)
+                side_of[key] = s
+                le.append(e); ls.append(k); re.append(bnd.get(key, -1)); rs.append(-1)
+            es[e, k] = s
+    le, re, ls, rs = (np.array(x, dtype=np.int64) for x in (le, re, ls, rs))
+    order = np.concatenate([np.nonzero(re == t)[0] for t in (-1, -2, -3)] + [np.nonzero(re >= 0)[0]])
+    inv = np.empty_like(order)
+    inv[order] = np.arange(order.size)
+    es = inv[es]
+    T = np.array(tris)
+    V = [xy[T[:, 0], 0], xy[T[:, 0], 1], xy[T[:, 1], 0], xy[T[:, 1], 1], xy[T[:, 2], 0], xy[T[:, 2], 1]]
+    m = Mesh(*V, es[:, 0], es[:, 1], es[:, 2], le[order], re[order], ls[order], rs[order],
+             meta=dict(kind="gmsh"))
+    m.check()
+    return m

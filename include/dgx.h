@@ -116,6 +116,16 @@ int dgx_periodic_square_arrays(int n, double lx, double ly, double x0, double y0
 int dgx_mesh_create_periodic_square(int n, double lx, double ly, double x0, double y0,
                                     double jitter, unsigned long long seed, dgx_mesh **out);
 int dgx_mesh_destroy(dgx_mesh *mesh);
+/* The reference's .pmsh text format (read_mesh, src/2d/conservation/conserv.cu:
+ * 118-192; written by src/2d/genmesh.py:290-308).  dgx_pmsh_info gives the
+ * counts, dgx_pmsh_read fills caller arrays V[6][E], elem_s[3][E], sides[4][S]
+ * (left_elem, right_elem, left_side, right_side); dgx_pmsh_write writes
+ * full-precision coordinates. */
+int dgx_pmsh_info(const char *path, int *num_elem, int *num_sides);
+int dgx_pmsh_read(const char *path, double *V, int *elem_s, int *sides);
+int dgx_pmsh_write(const char *path, int num_elem, int num_sides, const double *V,
+                   const int *elem_s, const int *sides);
+int dgx_mesh_create_from_pmsh(const char *path, dgx_mesh **out);
 /* FP64 geometric factors copied to host arrays (NULL to skip): J, x_r, y_r,
  * x_s, y_s, inscribed diameter per element; length, Nx, Ny per side. */
 int dgx_mesh_geometry(const dgx_mesh *mesh, double *J, double *xr, double *yr, double *xs,
@@ -191,6 +201,10 @@ int dgx_conserved_totals_static(const dgx_solver *solver, const void *state, dou
                                 void *stream);
 /* Maximum cell-average wave speed of the resident state. */
 int dgx_max_wave_speed(dgx_solver *solver, double *out, void *stream);
+/* Vertex values of every variable as the reference's Gmsh "ST" views
+ * (src/2d/conservation/main.cu:193-209), one file per variable named by
+ * printf(path_pattern, variable), e.g. "output/U%d.msh". */
+int dgx_write_vertex_values(dgx_solver *solver, const char *path_pattern);
 /* Kernel options of a solver (for autotuning and tests):
  *   DGX_OPT_PREFETCH  1 (default): RK stages 2-4 copy the tile's base state and
  *                     accumulator into shared memory with the TMA engine while
