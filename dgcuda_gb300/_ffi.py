@@ -22,6 +22,7 @@ FP32, FP32_BF16X3, FP64 = 0, 1, 2
 RK4 = 0
 DT_FIXED, DT_CFL = 0, 1
 OPT_PREFETCH = 1
+BC_NONE, BC_FREESTREAM, BC_EXACT = 0, 1, 2
 IC_GAUSSIAN, IC_POLY, IC_DENSITY_WAVE, IC_VORTEX, IC_CONSTANT = 0, 1, 2, 3, 4
 
 
@@ -98,6 +99,7 @@ SIGNATURES = {
     "dgx_max_wave_speed": (None, [_vp, _dp, _vp]),
     "dgx_launch_count": (None, [_vp, C.POINTER(C.c_longlong)]),
     "dgx_solver_set_option": (None, [_vp, _i, _i]),
+    "dgx_solver_set_boundary": (None, [_vp, _i, _i, _dp]),
     "dgx_batch_create": (None, [C.POINTER(_vp), _i, C.POINTER(_vp)]),
     "dgx_batch_destroy": (None, [_vp]),
     "dgx_batch_step": (None, [_vp, _vp]),

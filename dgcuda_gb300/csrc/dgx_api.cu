@@ -159,6 +159,14 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
     a.scal = s.scal;
     a.dt = dt;
     a.t = t;
+    static const double kStageC[5] = {0.0, 0.0, 0.5, 0.5, 1.0};   // RK4 stage times
+    a.stage_c = kStageC[mode < 0 || mode > 4 ? 0 : mode];
+    a.bc_kind = s.bc_kind;
+    a.bc_ic = s.bc_ic;
+    for (int i = 0; i < 4; ++i) a.bc_state[i] = s.bc_state[i];
+    for (int i = 0; i < 8; ++i) a.bc_params[i] = s.bc_params[i];
+    a.vx1 = m.V;
+    a.vy1 = m.V + m.num_elem;
     if (s.precision == DGX_FP64) {
         a.geo = m.geo64;
         a.fn = m.fn64;
@@ -351,10 +359,6 @@ int dgx_solver_create(dgx_mesh *mesh, const dgx_solver_desc *desc, dgx_solver **
     }
     if (desc->integrator != DGX_RK4) { set_error("integrator %d is not served by this build", desc->integrator); return DGX_ERR_UNSUPPORTED; }
     if (desc->equation == DGX_EULER && !(desc->gamma > 1.0)) { set_error("gamma must be > 1"); return DGX_ERR_INVALID; }
-    if (mesh->d.num_boundary > 0) {
-        set_error("meshes with boundary sides are not served by this build (periodic meshes only)");
-        return DGX_ERR_UNSUPPORTED;
-    }
     int rc = ensure_device_tables();
     if (rc) return rc;
     dgx_solver *sv = new (std::nothrow) dgx_solver();
@@ -596,6 +600,35 @@ int dgx_conserved_totals(dgx_solver *sv, double *out, void *stream) {
     int rc = conserved_totals(sv->s, sv->mesh->d, out, as_stream(stream));
     if (!rc) sv->launches += 2 * sv->s.nv * 2;
     return rc;
+}
+
+int dgx_solver_set_boundary(dgx_solver *sv, int kind, int ic, const double *params) {
+    if (!sv) return DGX_ERR_INVALID;
+    SolverDev &s = sv->s;
+    switch (kind) {
+    case DGX_BC_NONE: s.bc_kind = 0; return DGX_OK;
+    case DGX_BC_FREESTREAM: {
+        if (s.equation != DGX_EULER || !params) { set_error("the free-stream state needs the Euler equations and {rho, u, v, p}"); return DGX_ERR_INVALID; }
+        const double rho = params[0], u = params[1], v = params[2], p = params[3];
+        if (!(rho > 0) || !(p > 0)) { set_error("free-stream density and pressure must be positive"); return DGX_ERR_INVALID; }
+        s.bc_state[0] = rho;
+        s.bc_state[1] = rho * u;
+        s.bc_state[2] = rho * v;
+        s.bc_state[3] = p / (s.gamma - 1.0) + 0.5 * rho * (u * u + v * v);
+        s.bc_kind = 1;
+        return DGX_OK;
+    }
+    case DGX_BC_EXACT:
+        if (s.equation != DGX_ADVECTION || ic < DGX_IC_GAUSSIAN || ic > DGX_IC_POLY) {
+            set_error("the exact Dirichlet boundary needs advection and a scalar initial condition");
+            return DGX_ERR_INVALID;
+        }
+        s.bc_ic = ic;
+        for (int i = 0; i < 8; ++i) s.bc_params[i] = params ? params[i] : 0.0;
+        s.bc_kind = 2;
+        return DGX_OK;
+    default: set_error("unknown boundary kind %d", kind); return DGX_ERR_INVALID;
+    }
 }
 
 int dgx_solver_set_option(dgx_solver *sv, int option, int value) {

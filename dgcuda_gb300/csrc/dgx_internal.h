@@ -103,6 +103,9 @@ struct SolverDev {
     int red_len = 0;
     int dt_mode = DGX_DT_CFL;
     int prefetch = 1;                  // DGX_OPT_PREFETCH
+    int bc_kind = 0, bc_ic = 0;        // boundary ghost states (StageArgs)
+    double bc_state[4] = {0, 0, 0, 0};
+    double bc_params[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 }  // namespace dgx
@@ -141,6 +144,14 @@ struct StageArgs {
     const void *fn;
     const double *scal;   // device dt/t (modes 1..4); may be null for mode 0
     double dt, t;         // host dt/t for mode 0
+    double stage_c;       // stage time = step start + stage_c * dt (modes 1..4)
+    // boundary ghost states: bc_kind 0 none (interior state), 1 free-stream
+    // state bc_state (Euler), 2 exact initial condition bc_ic / bc_params
+    // translated by a*t (advection)
+    int bc_kind, bc_ic;
+    double bc_state[4];
+    double bc_params[8];
+    const double *vx1, *vy1;   // first vertex of every element (FP64)
 };
 
 // Batched launch: items[i] = (index into args, tile); grid CTAs walk the list.

@@ -25,6 +25,7 @@
 // the result does not depend on scheduling.
 #pragma once
 
+#include "dgx_ic.cuh"
 #include "dgx_internal.h"
 
 #ifndef DGX_REAL
@@ -61,6 +62,7 @@ struct Lay {
     static constexpr int SIDE = GY + NP * NQ;
     static constexpr int LIFT = SIDE + 3 * NP * NQ1;
     static constexpr int W1 = LIFT + 3 * NP * NQ1;
+    static constexpr int SRS = W1 + NQ1;
 };
 
 using R = DGX_REAL;
@@ -157,6 +159,52 @@ __device__ __forceinline__ void num_flux(const R *UL, const R *UR, R nx, R ny, i
                          (UR[3] + pr) * unr};
 #pragma unroll
         for (int n = 0; n < 4; ++n) Fh[n] = R(0.5) * ((fl[n] + fr[n]) + lam * (UL[n] - UR[n]));
+    }
+}
+
+// Ghost state on a boundary side (the element is the side's left element, n
+// points out of the domain), at the side's point j in this element's order:
+//   Euler  -1 reflecting: density and energy kept, momentum reduced to its
+//             tangential part (the reference's reflecting_boundary,
+//             src/2d/conservation/euler/cylinder/cylinder.cu:58-111, with the
+//             side's normal);
+//          -2 outflow, -3 inflow: the solver's free-stream state (the problem
+//             hooks U_outflow / U_inflow, src/2d/conservation/euler/euler.cu:177-241),
+//             or the interior state when none is set;
+//   advection: the initial condition translated by a*t (the reference's
+//             boundary_exact, src/2d/2dadvec/2dadvec_kernels.cu:184-186,492-517),
+//             or the interior state when none is set.
+template <int P, int EQ>
+__device__ __noinline__ void boundary_ghost(const StageArgs &a, int tag, int k, int j, int e, const R *UO,
+                                            R nx, R ny, R xr, R yr, R xs, R ys, R *UN) {
+    using L = Lay<P>;
+    constexpr int NQ1 = L::NQ1;
+    constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
+    if constexpr (EQ == DGX_EULER) {
+        if (tag == -1) {
+            const R mn = UO[1] * nx + UO[2] * ny;
+            UN[0] = UO[0];
+            UN[1] = UO[1] - mn * nx;
+            UN[2] = UO[2] - mn * ny;
+            UN[3] = UO[3];
+        } else if (a.bc_kind == 1) {
+            for (int n = 0; n < 4; ++n) UN[n] = R(a.bc_state[n]);
+        } else {
+            for (int n = 0; n < 4; ++n) UN[n] = UO[n];
+        }
+    } else {
+        if (a.bc_kind == 2) {
+            const double r = static_cast<double>(c_tab[L::SRS + (k * NQ1 + j) * 2]);
+            const double s = static_cast<double>(c_tab[L::SRS + (k * NQ1 + j) * 2 + 1]);
+            const double x = a.vx1[e] + static_cast<double>(xr) * r + static_cast<double>(xs) * s;
+            const double y = a.vy1[e] + static_cast<double>(yr) * r + static_cast<double>(ys) * s;
+            const double t = a.mode == 0 ? a.t : a.scal[2] + a.stage_c * a.scal[0];
+            double U[4];
+            ic_eval(a.bc_ic, a.bc_params, a.gamma, x - a.ax * t, y - a.ay * t, U);
+            UN[0] = static_cast<R>(U[0]);
+        } else {
+            for (int n = 0; n < NV; ++n) UN[n] = UO[n];
+        }
     }
 }
 
@@ -337,12 +385,14 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
 #pragma unroll
         for (int i = 0; i < NP; ++i) rhs[n][i] = R(0);
 
-    R invJ = R(0);
+    R invJ = R(0), xr = R(0), yr = R(0), xs = R(0), ys = R(0);
     if (live) {
         const R *__restrict__ geo = static_cast<const R *>(a.geo);
         invJ = __ldg(geo + e);
-        const R xr = __ldg(geo + SE + e), yr = __ldg(geo + 2 * SE + e);
-        const R xs = __ldg(geo + 3 * SE + e), ys = __ldg(geo + 4 * SE + e);
+        xr = __ldg(geo + SE + e);
+        yr = __ldg(geo + 2 * SE + e);
+        xs = __ldg(geo + 3 * SE + e);
+        ys = __ldg(geo + 4 * SE + e);
         // ---- volume integral ----------------------------------------------------
 #if DGX_ROLLED_VOLUME
 #pragma unroll 1
@@ -386,9 +436,9 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
         const R nx = pick3(snx[0], snx[1], snx[2], k), ny = pick3(sny[0], sny[1], sny[2], k);
         const R hl = pick3(shl[0], shl[1], shl[2], k);
         const int own = 3 * tid + k;
-        // a boundary side (rejected at solver creation) would mirror the own trace
-        const int slot = word >= 0 ? (word >> 1) : own;
-        const int il = word >= 0 ? (word & 1) : 1;
+        const bool bnd = word < 0;              // boundary side: this element is its left element
+        const int slot = bnd ? own : (word >> 1);
+        const int il = bnd ? 1 : (word & 1);
         const R *s_own = s_tr + own * TSW;
         const R *s_nbr = s_tr + slot * TSW;
         R Fh[NQ1][NV];
@@ -399,6 +449,10 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
             for (int n = 0; n < NV; ++n) {
                 UO[n] = s_own[j * NV + n];
                 UN[n] = s_nbr[(NQ1 - 1 - j) * NV + n];
+            }
+            if (bnd) boundary_ghost<P, EQ>(a, word, k, j, e, UO, nx, ny, xr, yr, xs, ys, UN);
+#pragma unroll
+            for (int n = 0; n < NV; ++n) {
                 UL[n] = il ? UO[n] : UN[n];
                 UR[n] = il ? UN[n] : UO[n];
             }
@@ -647,6 +701,16 @@ static int upload_tables_impl() {
                     lf[o] = static_cast<R>(T.w1[j] * T.side[o]);
                 }
         for (int j = 0; j < nq1; ++j) w1[j] = static_cast<R>(T.w1[j]);
+        // side points in the reference orientation (side 0: V1->V2, 1: V2->V3, 2: V3->V1)
+        R *srs = w1 + nq1;
+        for (int j = 0; j < nq1; ++j) {
+            const double g = T.s1[j], gr = T.s1[nq1 - 1 - j];
+            const double rs[3][2] = {{0.5 + 0.5 * g, 0.0}, {(1.0 - g) / 2.0, (1.0 + g) / 2.0}, {0.0, 0.5 + 0.5 * gr}};
+            for (int sd = 0; sd < 3; ++sd) {
+                srs[(sd * nq1 + j) * 2] = static_cast<R>(rs[sd][0]);
+                srs[(sd * nq1 + j) * 2 + 1] = static_cast<R>(rs[sd][1]);
+            }
+        }
     }
     DGX_TRY_CUDA(cudaMemcpyToSymbol(c_tab, host, sizeof(host)));
     return DGX_OK;

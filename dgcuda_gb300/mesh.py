@@ -23,7 +23,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 __all__ = ["Mesh", "periodic_square", "scramble", "dirichlet_square", "unit_draws", "write_pmsh",
-           "read_pmsh", "read_gmsh"]
+           "read_pmsh", "read_gmsh", "tag_boundary"]
 
 
 def _splitmix64(x: np.ndarray) -> np.ndarray:
@@ -365,3 +365,16 @@ def read_gmsh(path_or_text: str, boundary_tags=None) -> Mesh:
              meta=dict(kind="gmsh"))
     m.check()
     return m
+
+
+def tag_boundary(mesh: Mesh, fn) -> Mesh:
+    """Re-tag boundary sides by position: fn(x_mid, y_mid) -> tag in {-1, -2, -3}
+    for each boundary side's midpoint.  Returns a new Mesh."""
+    V = np.stack(mesh.vertices()).reshape(3, 2, -1)
+    re = mesh.right_elem.astype(np.int64).copy()
+    for s in np.nonzero(re < 0)[0]:
+        L, ls = mesh.left_elem[s], mesh.left_side[s]
+        a, b = V[ls, :, L], V[(ls + 1) % 3, :, L]
+        re[s] = int(fn(0.5 * (a[0] + b[0]), 0.5 * (a[1] + b[1])))
+    return Mesh(*mesh.vertices(), *mesh.elem_sides(), mesh.left_elem, re, mesh.left_side,
+                mesh.right_side, meta=dict(mesh.meta, tagged=True))

@@ -200,6 +200,11 @@ class Solver:
         call("dgx_max_wave_speed", self.h, C.byref(v), stream)
         return v.value
 
+    def set_boundary(self, kind: int, ic: int = 0, params=()) -> None:
+        P = np.zeros(8)
+        P[:len(params)] = params
+        call("dgx_solver_set_boundary", self.h, int(kind), int(ic), _dp(P))
+
     def set_option(self, option: int, value: int) -> None:
         call("dgx_solver_set_option", self.h, int(option), int(value))
 

@@ -205,6 +205,17 @@ int dgx_max_wave_speed(dgx_solver *solver, double *out, void *stream);
  * (src/2d/conservation/main.cu:193-209), one file per variable named by
  * printf(path_pattern, variable), e.g. "output/U%d.msh". */
 int dgx_write_vertex_values(dgx_solver *solver, const char *path_pattern);
+/* Boundary sides (right_elem < 0, the element being the side's left element):
+ *   Euler, -1 reflecting: density and energy kept, momentum reduced to its
+ *     tangential part (the reference's reflecting_boundary,
+ *     src/2d/conservation/euler/cylinder/cylinder.cu:58-111, with the side normal);
+ *   Euler, -2 outflow / -3 inflow: DGX_BC_FREESTREAM params {rho, u, v, p}
+ *     (the problem hooks U_outflow / U_inflow, euler.cu:177-241);
+ *   advection, any tag: DGX_BC_EXACT, the initial condition `ic` with `params`
+ *     translated by a*t (the reference's boundary_exact, 2dadvec_kernels.cu:184-186).
+ * Without a setting, outflow/inflow and advection sides take the interior state. */
+enum dgx_bc { DGX_BC_NONE = 0, DGX_BC_FREESTREAM = 1, DGX_BC_EXACT = 2 };
+int dgx_solver_set_boundary(dgx_solver *solver, int kind, int ic, const double *params);
 /* Kernel options of a solver (for autotuning and tests):
  *   DGX_OPT_PREFETCH  1 (default): RK stages 2-4 copy the tile's base state and
  *                     accumulator into shared memory with the TMA engine while

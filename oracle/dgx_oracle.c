@@ -291,7 +291,14 @@ typedef struct {
     double *left_rhs, *right_rhs, *quad_rhs;    /* [n][i][side] / [n][i][elem] */
     double *k[4], *kstar;
     double min_diam;
+    /* boundary ghost states: 0 none (interior state), 1 free-stream state
+     * (Euler inflow/outflow), 2 exact initial condition translated by a*t
+     * (advection) */
+    int bc_kind, bc_ic;
+    double bc_state[4], bc_params[8];
 } orc_solver;
+
+void orc_ic_eval(int ic, const double *P, double g, double x, double y, double *U);
 
 static double orc_fsqrt(const orc_solver *S, double x) {
     return S->ref_sqrtf ? (double)sqrtf((float)x) : sqrt(x);
@@ -463,6 +470,55 @@ static void orc_phys_flux(const orc_solver *S, const double *U, double *fx, doub
     else orc_euler_flux(S->gamma, U, fx, fy);
 }
 
+/* Ghost state of a boundary side at its point j (the element is the side's
+ * left element, n points out of the domain): Euler -1 reflecting keeps density
+ * and energy and keeps the tangential momentum only (reflecting_boundary,
+ * src/2d/conservation/euler/cylinder/cylinder.cu:58-111, with the side normal);
+ * -2 outflow / -3 inflow take the free-stream state (U_outflow / U_inflow,
+ * euler.cu:177-241) or the interior state; advection takes the initial
+ * condition translated by a*t (boundary_exact, 2dadvec_kernels.cu:184-186) or
+ * the interior state. */
+static void orc_ghost(const orc_solver *S, int tag, int L, int ls, int j, double t, const double *UL,
+                      double nx, double ny, double *UR) {
+    int n;
+    if (S->eq == ORC_EULER) {
+        if (tag == -1) {
+            double mn = UL[1] * nx + UL[2] * ny;
+            UR[0] = UL[0]; UR[1] = UL[1] - mn * nx; UR[2] = UL[2] - mn * ny; UR[3] = UL[3];
+        } else if (S->bc_kind == 1) {
+            for (n = 0; n < 4; n++) UR[n] = S->bc_state[n];
+        } else {
+            for (n = 0; n < 4; n++) UR[n] = UL[n];
+        }
+    } else if (S->bc_kind == 2) {
+        const orc_tables *T = &S->T;
+        double g = T->s1[j], gr = T->s1[T->nq1 - 1 - j], r, s, x, y, U[4];
+        if (ls == 0) { r = 0.5 + 0.5 * g; s = 0.0; }
+        else if (ls == 1) { r = (1.0 - g) / 2.0; s = (1.0 + g) / 2.0; }
+        else { r = 0.0; s = 0.5 + 0.5 * gr; }
+        x = S->V[0][L] + S->xr[L] * r + S->xs[L] * s;
+        y = S->V[1][L] + S->yr[L] * r + S->ys[L] * s;
+        orc_ic_eval(S->bc_ic, S->bc_params, S->gamma, x - S->ax * t, y - S->ay * t, U);
+        UR[0] = U[0];
+    } else {
+        UR[0] = UL[0];
+    }
+}
+
+int orc_set_boundary(orc_solver *S, int kind, int ic, const double *params) {
+    int i;
+    if (kind == 1) {
+        double rho = params[0], u = params[1], v = params[2], p = params[3];
+        S->bc_state[0] = rho; S->bc_state[1] = rho * u; S->bc_state[2] = rho * v;
+        S->bc_state[3] = p / (S->gamma - 1.0) + 0.5 * rho * (u * u + v * v);
+    } else if (kind == 2) {
+        S->bc_ic = ic;
+        for (i = 0; i < 8; i++) S->bc_params[i] = params ? params[i] : 0.0;
+    }
+    S->bc_kind = kind;
+    return 0;
+}
+
 /* ------------------------------------------------------------------------- */
 /* RHS: k = dt / J * (volume + sum of the three lifted edge fluxes)           */
 /* ------------------------------------------------------------------------- */
@@ -471,7 +527,6 @@ int orc_rhs(orc_solver *S, const double *u, double *k, double dt, double t) {
     int np = T->np, nq = T->nq, nq1 = T->nq1, nv = S->nv;
     int E = S->num_elem, Sd = S->num_sides;
     int s, e, bad = 0;
-    (void)t;
     /* surface pass, one edge at a time (conserv_kernels.cu:697-758) */
 #pragma omp parallel for schedule(static) reduction(| : bad)
     for (s = 0; s < Sd; s++) {
@@ -479,19 +534,19 @@ int orc_rhs(orc_solver *S, const double *u, double *k, double dt, double t) {
         double cL[ORC_MAXV][ORC_MAXNP], cR[ORC_MAXV][ORC_MAXNP];
         double Fh[ORC_MAXQ1][ORC_MAXV];
         int i, j, n;
-        if (R < 0) { bad |= 1; continue; } /* boundary ghost states are problem hooks */
         for (n = 0; n < nv; n++)
             for (i = 0; i < np; i++) {
                 cL[n][i] = u[(size_t)E * np * n + (size_t)i * E + L];
-                cR[n][i] = u[(size_t)E * np * n + (size_t)i * E + R];
+                cR[n][i] = R >= 0 ? u[(size_t)E * np * n + (size_t)i * E + R] : 0.0;
             }
         for (j = 0; j < nq1; j++) {
             double UL[ORC_MAXV] = {0}, UR[ORC_MAXV] = {0};
             for (i = 0; i < np; i++)
                 for (n = 0; n < nv; n++) {
                     UL[n] += cL[n][i] * T->side[ls * np * nq1 + i * nq1 + j];
-                    UR[n] += cR[n][i] * T->side[rs * np * nq1 + i * nq1 + nq1 - j - 1];
+                    if (R >= 0) UR[n] += cR[n][i] * T->side[rs * np * nq1 + i * nq1 + nq1 - j - 1];
                 }
+            if (R < 0) orc_ghost(S, R, L, ls, j, t, UL, S->nx[s], S->ny[s], UR);
             orc_num_flux(S, UL, UR, S->nx[s], S->ny[s], Fh[j]);
         }
         for (i = 0; i < np; i++)

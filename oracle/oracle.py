@@ -67,6 +67,7 @@ def lib():
         L.orc_totals.argtypes = [C.c_void_p, _dp, _dp]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_ic_eval.argtypes = [C.c_int, _dp, C.c_double, C.c_double, C.c_double, _dp]
+        L.orc_set_boundary.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp]
         _lib = L
     return _lib
 
@@ -153,6 +154,12 @@ class Oracle:
         if rc:
             raise RuntimeError(f"orc_rhs failed ({rc})")
         return k
+
+    def set_boundary(self, kind: int, ic: int = 0, params=()) -> None:
+        """0 none, 1 free-stream state {rho, u, v, p}, 2 exact IC translated by a*t."""
+        P = np.zeros(8)
+        P[:len(params)] = params
+        lib().orc_set_boundary(self.h, int(kind), int(ic), P)
 
     def max_lambda(self, c) -> float:
         return lib().orc_max_lambda(self.h, self._state(c))
