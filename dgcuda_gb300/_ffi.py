@@ -19,9 +19,10 @@ ERR_NONFINITE, ERR_BUSY, ERR_NOT_FOUND, ERR_TIMEOUT = -5, -6, -7, -8
 ADVECTION, EULER = 0, 1
 FLUX_CENTRAL, FLUX_LLF = 0, 1
 FP32, FP32_BF16X3, FP64 = 0, 1, 2
-RK4 = 0
+RK4, RK2, FE = 0, 1, 2
 DT_FIXED, DT_CFL = 0, 1
-OPT_PREFETCH = 1
+OPT_PREFETCH, OPT_STAGE_TIME = 1, 2
+STAGE_TIME_EXACT, STAGE_TIME_REFERENCE = 0, 1
 BC_NONE, BC_FREESTREAM, BC_EXACT = 0, 1, 2
 IC_GAUSSIAN, IC_POLY, IC_DENSITY_WAVE, IC_VORTEX, IC_CONSTANT = 0, 1, 2, 3, 4
 

@@ -110,11 +110,31 @@ int stage_launch(dgx_solver *sv, int mode, const void *u, const void *c, void *a
 int run_stage(dgx_solver *sv, int stage, cudaStream_t st) {
     SolverDev &s = sv->s;
     int rc;
-    switch (stage) {
-    case 0:
+    const int nst = num_stages(s.integrator);
+    if (stage < 0 || stage >= nst) { set_error("stage must be 0..%d", nst - 1); return DGX_ERR_INVALID; }
+    if (stage == 0) {
         rc = launch_dt(s, sv->mesh->d, st);
         if (rc) return rc;
         sv->launches++;
+    }
+    if (s.integrator == DGX_RK2) {
+        // k1 at the state, ua = c + k1/2; then c += k2 with k2 at ua
+        // (rk2_tempstorage / rk2, time_integrator.cu:445-464, 518-580)
+        if (stage == 0) return stage_launch(sv, 5, s.c, nullptr, nullptr, s.ua, 0.0, 0.0, st);
+        return stage_launch(sv, 6, s.ua, s.c, nullptr, s.c, 0.0, 0.0, st);
+    }
+    if (s.integrator == DGX_FE) {
+        // ua = c + k, then commit ua to c (neighbouring tiles read c while the
+        // stage runs, so it cannot be updated in place; eval_rhs_fe,
+        // time_integrator.cu:622-700)
+        rc = stage_launch(sv, 5, s.c, nullptr, nullptr, s.ua, 0.0, 0.0, st);
+        if (rc) return rc;
+        rc = commit_state(s, s.c, s.ua, st);
+        if (!rc) sv->launches++;
+        return rc;
+    }
+    switch (stage) {
+    case 0:
         return stage_launch(sv, 1, s.c, s.c, s.acc, s.ua, 0.0, 0.0, st);
     case 1: return stage_launch(sv, 2, s.ua, s.c, s.acc, s.ub, 0.0, 0.0, st);
     case 2: return stage_launch(sv, 3, s.ub, s.c, s.acc, s.ua, 0.0, 0.0, st);
@@ -146,7 +166,7 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
     a.ayf = static_cast<float>(s.ay);
     // plane starts are 16-byte aligned when E * sizeof(value) is a multiple of 16
     a.prefetch = s.prefetch && (static_cast<size_t>(m.num_elem) * elem_size(s)) % 16 == 0 &&
-                 mode >= 2 && c && acc;
+                 mode >= 2 && mode <= 4 && c && acc;
     a.status = s.status;
     a.u = u;
     a.c = c;
@@ -159,8 +179,14 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
     a.scal = s.scal;
     a.dt = dt;
     a.t = t;
-    static const double kStageC[5] = {0.0, 0.0, 0.5, 0.5, 1.0};   // RK4 stage times
-    a.stage_c = kStageC[mode < 0 || mode > 4 ? 0 : mode];
+    // stage node c_s by kernel mode: RK4 (1..4) 0, 1/2, 1/2, 1; RK2 (5, 6) 0,
+    // 1/2; forward Euler (5) 0
+    static const double kNode[7] = {0.0, 0.0, 0.5, 0.5, 1.0, 0.0, 0.5};
+    double node = kNode[mode < 0 || mode > 6 ? 0 : mode];
+    if (s.stage_time == DGX_STAGE_TIME_REFERENCE)   // t_{n+1} + c_s dt (Euler RK4/RK2) or t_n
+        node = (s.equation == DGX_EULER && s.integrator != DGX_FE) ? 1.0 + node : 0.0;
+    a.stage_c = node;
+    a.alpha = (mode == 5 && s.integrator == DGX_RK2) ? 0.5 : 1.0;
     a.bc_kind = s.bc_kind;
     a.bc_ic = s.bc_ic;
     for (int i = 0; i < 4; ++i) a.bc_state[i] = s.bc_state[i];
@@ -357,7 +383,10 @@ int dgx_solver_create(dgx_mesh *mesh, const dgx_solver_desc *desc, dgx_solver **
         set_error("precision %d is not served by this build", desc->precision);
         return DGX_ERR_UNSUPPORTED;
     }
-    if (desc->integrator != DGX_RK4) { set_error("integrator %d is not served by this build", desc->integrator); return DGX_ERR_UNSUPPORTED; }
+    if (desc->integrator != DGX_RK4 && desc->integrator != DGX_RK2 && desc->integrator != DGX_FE) {
+        set_error("unknown integrator %d", desc->integrator);
+        return DGX_ERR_INVALID;
+    }
     if (desc->equation == DGX_EULER && !(desc->gamma > 1.0)) { set_error("gamma must be > 1"); return DGX_ERR_INVALID; }
     int rc = ensure_device_tables();
     if (rc) return rc;
@@ -373,17 +402,20 @@ int dgx_solver_create(dgx_mesh *mesh, const dgx_solver_desc *desc, dgx_solver **
     s.gamma = desc->gamma;
     s.ax = desc->ax;
     s.ay = desc->ay;
+    s.integrator = desc->integrator;
     s.n = static_cast<size_t>(s.nv) * s.np * mesh->d.num_elem;
     const size_t es = elem_size(s);
     size_t acct = 0;
+    // c and ua for every integrator; RK4 adds its accumulator and a second stage input
     char *bufs[4] = {nullptr, nullptr, nullptr, nullptr};
-    for (int i = 0; i < 4 && !rc; ++i) rc = dalloc(&bufs[i], s.n * es, &acct);
+    const int nbuf = s.integrator == DGX_RK4 ? 4 : 2;
+    for (int i = 0; i < nbuf && !rc; ++i) rc = dalloc(&bufs[i], s.n * es, &acct);
     if (!rc) rc = dalloc(&s.scal, 8, &acct);
     if (!rc) rc = dalloc(&s.lam_bits, 1, &acct);
     if (!rc) rc = dalloc(&s.counter, 1, &acct);
     if (!rc) rc = dalloc(&s.status, 1, &acct);
     if (!rc) rc = dalloc(&s.steps, 1, &acct);
-    s.c = bufs[0]; s.acc = bufs[1]; s.ua = bufs[2]; s.ub = bufs[3];
+    s.c = bufs[0]; s.ua = bufs[1]; s.acc = bufs[2]; s.ub = bufs[3];
     if (!rc) {
         const double init[8] = {0.0, 0.0, 0.0, 0.0, 0.7, 0.0, 0.0, 0.0};
         cudaError_t ce = cudaMemcpy(s.scal, init, sizeof(init), cudaMemcpyHostToDevice);
@@ -461,9 +493,9 @@ int dgx_set_state_f32(dgx_solver *sv, const float *c, void *stream) {
         DGX_TRY_CUDA(cudaMemcpyAsync(s.c, c, s.n * sizeof(float), cudaMemcpyHostToDevice, as_stream(stream)));
         return DGX_OK;
     }
-    // stage through the accumulator buffer, then widen on the device
-    DGX_TRY_CUDA(cudaMemcpyAsync(s.acc, c, s.n * sizeof(float), cudaMemcpyHostToDevice, as_stream(stream)));
-    return convert_state(s.acc, 0, s.c, 1, s.n, as_stream(stream));
+    // stage through the (between steps unused) stage-input buffer, then widen on the device
+    DGX_TRY_CUDA(cudaMemcpyAsync(s.ua, c, s.n * sizeof(float), cudaMemcpyHostToDevice, as_stream(stream)));
+    return convert_state(s.ua, 0, s.c, 1, s.n, as_stream(stream));
 }
 
 int dgx_get_state_f32(dgx_solver *sv, float *c, void *stream) {
@@ -473,9 +505,9 @@ int dgx_get_state_f32(dgx_solver *sv, float *c, void *stream) {
         DGX_TRY_CUDA(cudaMemcpyAsync(c, s.c, s.n * sizeof(float), cudaMemcpyDeviceToHost, as_stream(stream)));
         return DGX_OK;
     }
-    int rc = convert_state(s.c, 1, s.acc, 0, s.n, as_stream(stream));
+    int rc = convert_state(s.c, 1, s.ua, 0, s.n, as_stream(stream));
     if (rc) return rc;
-    DGX_TRY_CUDA(cudaMemcpyAsync(c, s.acc, s.n * sizeof(float), cudaMemcpyDeviceToHost, as_stream(stream)));
+    DGX_TRY_CUDA(cudaMemcpyAsync(c, s.ua, s.n * sizeof(float), cudaMemcpyDeviceToHost, as_stream(stream)));
     return DGX_OK;
 }
 
@@ -487,12 +519,12 @@ int dgx_state_device_ptr(dgx_solver *sv, void **ptr) {
 
 int dgx_project_ic(dgx_solver *sv, int ic, const double *params) {
     if (!sv) return DGX_ERR_INVALID;
-    if (ic < DGX_IC_GAUSSIAN || ic > DGX_IC_CONSTANT) { set_error("unknown initial condition %d", ic); return DGX_ERR_INVALID; }
+    if (ic < DGX_IC_GAUSSIAN || ic > DGX_IC_THREEPOINT) { set_error("unknown initial condition %d", ic); return DGX_ERR_INVALID; }
     if (sv->s.equation == DGX_EULER && (ic == DGX_IC_GAUSSIAN || ic == DGX_IC_POLY)) {
         set_error("initial condition %d is scalar", ic);
         return DGX_ERR_INVALID;
     }
-    if (sv->s.equation == DGX_ADVECTION && (ic == DGX_IC_DENSITY_WAVE || ic == DGX_IC_VORTEX)) {
+    if (sv->s.equation == DGX_ADVECTION && ic != DGX_IC_GAUSSIAN && ic != DGX_IC_POLY && ic != DGX_IC_CONSTANT) {
         set_error("initial condition %d needs the Euler equations", ic);
         return DGX_ERR_INVALID;
     }
@@ -532,7 +564,7 @@ int dgx_rk_stage(dgx_solver *sv, int stage, void *stream) {
 
 int dgx_step(dgx_solver *sv, void *stream) {
     if (!sv) return DGX_ERR_INVALID;
-    for (int st = 0; st < 4; ++st) {
+    for (int st = 0; st < num_stages(sv->s.integrator); ++st) {
         int rc = run_stage(sv, st, as_stream(stream));
         if (rc) return rc;
     }
@@ -627,6 +659,15 @@ int dgx_solver_set_boundary(dgx_solver *sv, int kind, int ic, const double *para
         for (int i = 0; i < 8; ++i) s.bc_params[i] = params ? params[i] : 0.0;
         s.bc_kind = 2;
         return DGX_OK;
+    case DGX_BC_PROBLEM:
+        if (s.equation != DGX_EULER || ic < DGX_IC_CYLINDER || ic > DGX_IC_THREEPOINT || !params) {
+            set_error("problem boundaries need the Euler equations, a problem initial condition and its params");
+            return DGX_ERR_INVALID;
+        }
+        s.bc_ic = ic;
+        for (int i = 0; i < 8; ++i) s.bc_params[i] = params[i];
+        s.bc_kind = 3;
+        return DGX_OK;
     default: set_error("unknown boundary kind %d", kind); return DGX_ERR_INVALID;
     }
 }
@@ -635,6 +676,13 @@ int dgx_solver_set_option(dgx_solver *sv, int option, int value) {
     if (!sv) return DGX_ERR_INVALID;
     switch (option) {
     case DGX_OPT_PREFETCH: sv->s.prefetch = value ? 1 : 0; return DGX_OK;
+    case DGX_OPT_STAGE_TIME:
+        if (value != DGX_STAGE_TIME_EXACT && value != DGX_STAGE_TIME_REFERENCE) {
+            set_error("unknown stage-time rule %d", value);
+            return DGX_ERR_INVALID;
+        }
+        sv->s.stage_time = value;
+        return DGX_OK;
     default: set_error("unknown option %d", option); return DGX_ERR_INVALID;
     }
 }

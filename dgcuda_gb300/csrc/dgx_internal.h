@@ -90,8 +90,8 @@ struct SolverDev {
     double gamma = 1.4, ax = 1.0, ay = 1.0;
     size_t n = 0;                      // values per state vector
     void *c = nullptr;                 // resident state (FP32 or FP64)
-    void *acc = nullptr;               // RK4 accumulator
-    void *ua = nullptr, *ub = nullptr; // stage inputs
+    void *acc = nullptr;               // RK4 accumulator (RK4 only)
+    void *ua = nullptr, *ub = nullptr; // stage inputs (ub: RK4 only)
     // device scalars: [0] dt of the current step, [1] t at the end of it,
     // [2] t at its start, [3] fixed dt, [4] cfl, [5] t_end, [6] max wave speed
     double *scal = nullptr;
@@ -102,6 +102,8 @@ struct SolverDev {
     double *red = nullptr;             // reduction scratch (partials)
     int red_len = 0;
     int dt_mode = DGX_DT_CFL;
+    int integrator = DGX_RK4;          // dgx_integrator
+    int stage_time = DGX_STAGE_TIME_EXACT;   // DGX_OPT_STAGE_TIME
     int prefetch = 1;                  // DGX_OPT_PREFETCH
     int bc_kind = 0, bc_ic = 0;        // boundary ghost states (StageArgs)
     double bc_state[4] = {0, 0, 0, 0};
@@ -126,7 +128,7 @@ int upload_tables_misc();
 
 struct StageArgs {
     int E;
-    int mode;          // 0 rhs, 1..4 RK4 stages
+    int mode;          // 0 rhs, 1..4 RK4 stages, 5 out = u + alpha k, 6 out = c + alpha k
     int flux;
     double gamma, ax, ay;
     float gammaf, axf, ayf;   // the same in FP32 (FP32 kernels)
@@ -144,7 +146,8 @@ struct StageArgs {
     const void *fn;
     const double *scal;   // device dt/t (modes 1..4); may be null for mode 0
     double dt, t;         // host dt/t for mode 0
-    double stage_c;       // stage time = step start + stage_c * dt (modes 1..4)
+    double stage_c;       // stage time = step start + stage_c * dt (modes 1..6)
+    double alpha;         // stage weight of modes 5 and 6
     // boundary ghost states: bc_kind 0 none (interior state), 1 free-stream
     // state bc_state (Euler), 2 exact initial condition bc_ic / bc_params
     // translated by a*t (advection)
@@ -194,6 +197,10 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
 int mesh_geometry(MeshDev &m, cudaStream_t st);
 int project_ic(const SolverDev &s, const MeshDev &m, int ic, const double *params, cudaStream_t st);
 int launch_dt(SolverDev &s, const MeshDev &m, cudaStream_t st);
+// dst = src (whole state vectors) when the current step advanced (dt != 0)
+int commit_state(const SolverDev &s, void *dst, const void *src, cudaStream_t st);
+// stages per step of an integrator
+inline int num_stages(int integrator) { return integrator == DGX_RK4 ? 4 : (integrator == DGX_RK2 ? 2 : 1); }
 int conserved_totals(SolverDev &s, const MeshDev &m, double *out, cudaStream_t st);
 int convert_state(const void *src, int src_is_double, void *dst, int dst_is_double, size_t n,
                   cudaStream_t st);

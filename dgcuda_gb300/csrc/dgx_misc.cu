@@ -391,4 +391,34 @@ int convert_state(const void *src, int src_is_double, void *dst, int dst_is_doub
     return DGX_OK;
 }
 
+// Forward Euler's commit of the new state: dst = src for `words` 32-bit words,
+// unless the step did not advance (dt == 0 at the end time: the stage kernel
+// then wrote nothing).  16-byte vectors when both ends are 16-byte aligned.
+__global__ void commit_kernel(const unsigned *__restrict__ src, unsigned *__restrict__ dst, size_t words,
+                              const double *__restrict__ scal) {
+    if (scal[0] == 0.0) return;
+    const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+    size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0;
+    size_t done = 0;
+    if (vec) {
+        const size_t nv = words / 4;
+        const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+        uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+        for (size_t j = i; j < nv; j += stride) d4[j] = s4[j];
+        done = nv * 4;
+    }
+    for (size_t j = done + i; j < words; j += stride) dst[j] = src[j];
+}
+
+int commit_state(const SolverDev &s, void *dst, const void *src, cudaStream_t st) {
+    const size_t words = s.n * (s.precision == DGX_FP64 ? 2 : 1);
+    int grid = blocks_for(words / 4 + 1);
+    if (grid > 152 * 8) grid = 152 * 8;
+    commit_kernel<<<grid, kThreads, 0, st>>>(static_cast<const unsigned *>(src), static_cast<unsigned *>(dst), words,
+                                             s.scal);
+    DGX_CHECK_LAUNCH();
+    return DGX_OK;
+}
+
 }  // namespace dgx

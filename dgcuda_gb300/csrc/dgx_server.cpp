@@ -73,6 +73,7 @@ struct dgx_server {
     std::deque<Request *> queue;
     std::map<long long, Request *> all;
     std::vector<Request *> active;
+    int in_transit = 0;   // admitted, out of the queue, not yet active or finished
     std::map<MeshKey, dgx_mesh *> meshes;     // shared meshes (refcounted by their solvers)
     std::vector<double> latencies;
     long long next_id = 1, submitted = 0, completed = 0, failed = 0, repacks = 0, steps = 0;
@@ -184,6 +185,7 @@ void worker_main(dgx_server *s) {
                 q->bytes = need;
                 s->in_use += need;
                 admit.push_back(q);
+                s->in_transit++;
             }
         }
         for (Request *q : admit) {
@@ -191,6 +193,7 @@ void worker_main(dgx_server *s) {
             dgx_mesh *m = cached_mesh(s, q->r, &rc);   // the cache is the worker's alone
             if (!rc) rc = start_solve(s, q, m);
             std::lock_guard<std::mutex> lk(s->mu);
+            s->in_transit--;
             if (rc) {
                 release_solve(s, q);
                 finish(s, q, kFailed, rc);
@@ -364,7 +367,7 @@ int dgx_server_wait_idle(dgx_server *s, double timeout_s) {
     if (!s) return DGX_ERR_INVALID;
     std::unique_lock<std::mutex> lk(s->mu);
     const bool ok = s->idle_cv.wait_for(lk, std::chrono::duration<double>(timeout_s),
-                                        [&] { return s->queue.empty() && s->active.empty(); });
+                                        [&] { return s->queue.empty() && s->active.empty() && s->in_transit == 0; });
     if (!ok) { set_error("server still busy after %.1f s", timeout_s); return DGX_ERR_TIMEOUT; }
     return DGX_OK;
 }

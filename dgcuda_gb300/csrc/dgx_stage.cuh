@@ -274,7 +274,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
 
     // modes 2..4 read the base state (2, 3) and the accumulator (2, 3, 4) at the
     // end: start their copies now
-    const bool pre = a.prefetch && a.mode >= 2;
+    const bool pre = a.prefetch && a.mode >= 2 && a.mode <= 4;
     if (pre && tid < 32) {
         // order this CTA's earlier generic-proxy accesses of the shared memory
         // (a previous tile) before the bulk copies that overwrite it
@@ -526,13 +526,37 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
             }
         break;
     }
-    default: {  // c = acc + k4/6
+    case 4: {   // c = acc + k4/6
 #pragma unroll
         for (int n = 0; n < NV; ++n)
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
                 const size_t o = (n * NP + i) * SE + e;
                 out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], pacc[(n * NP + i) * pstride]);
+            }
+        break;
+    }
+    case 5: {   // out = u + alpha k (RK2 first stage, forward Euler)
+        const R alpha = R(a.alpha);
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) out[(n * NP + i) * SE + e] = fma(alpha, sc * rhs[n][i], c[n][i]);
+        break;
+    }
+    default: {  // 6: out = c + alpha k (RK2 second stage).  out may be the base
+                // state itself: each thread reads and then writes only its own
+                // element's values, and no other thread reads them
+        const R alpha = R(a.alpha);
+        const R *pb = static_cast<const R *>(a.c) + e;
+        R *po = static_cast<R *>(a.out) + e;
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const size_t o = (n * NP + i) * SE;
+                const R base = pb[o];
+                po[o] = fma(alpha, sc * rhs[n][i], base);
             }
         break;
     }

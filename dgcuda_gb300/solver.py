@@ -96,9 +96,10 @@ class DeviceMesh:
 
 class Solver:
     def __init__(self, mesh, order: int, equation: int = _ffi.EULER, flux: int = _ffi.FLUX_LLF,
-                 precision: int = _ffi.FP32, gamma: float = 1.4, a=(1.0, 1.0)):
+                 precision: int = _ffi.FP32, gamma: float = 1.4, a=(1.0, 1.0),
+                 integrator: int = _ffi.RK4):
         self.dmesh = mesh if isinstance(mesh, DeviceMesh) else DeviceMesh(mesh)
-        desc = _ffi.SolverDesc(order, equation, flux, precision, _ffi.RK4, gamma, float(a[0]),
+        desc = _ffi.SolverDesc(order, equation, flux, precision, integrator, gamma, float(a[0]),
                                float(a[1]))
         h = C.c_void_p()
         call("dgx_solver_create", self.dmesh.h, C.byref(desc), C.byref(h))
@@ -108,6 +109,7 @@ class Solver:
         self.nv = 4 if equation == _ffi.EULER else 1
         self.E = self.dmesh.num_elem
         self.precision = precision
+        self.integrator = integrator
 
     @property
     def shape(self):

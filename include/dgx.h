@@ -46,7 +46,11 @@ enum dgx_status {
 enum dgx_equation { DGX_ADVECTION = 0, DGX_EULER = 1 };
 enum dgx_flux { DGX_FLUX_CENTRAL = 0, DGX_FLUX_LLF = 1 };
 enum dgx_precision { DGX_FP32 = 0, DGX_FP32_BF16X3 = 1, DGX_FP64 = 2 };
-enum dgx_integrator { DGX_RK4 = 0 };
+/* Time integrators (src/2d/conservation/time_integrator.cu):
+ *   RK4  classic four-stage Runge-Kutta (time_integrate_rk4, :221-434)
+ *   RK2  explicit midpoint: c += k(c + k(c)/2) (time_integrate_rk2, :466-614)
+ *   FE   forward Euler: c += k(c) (time_integrate_fe, :622-749) */
+enum dgx_integrator { DGX_RK4 = 0, DGX_RK2 = 1, DGX_FE = 2 };
 enum dgx_dt_mode { DGX_DT_FIXED = 0, DGX_DT_CFL = 1 };
 
 /* Built-in initial conditions (projected with the degree-2p rule, as the
@@ -56,13 +60,25 @@ enum dgx_dt_mode { DGX_DT_FIXED = 0, DGX_DT_CFL = 1 };
  *   DENSITY_WAVE  rho = 1 + A sin(2 pi k (x+y)), u, v, p  {A, u, v, p, k}
  *   VORTEX        isentropic vortex on a free stream      {x0, y0, beta, u, v, Lx, Ly}
  *   CONSTANT      constant state                          {rho, u, v, p} (advection: {u})
+ *   CYLINDER      free stream rho = gamma, u = M, v = 0, p = 1  {M}
+ *                 (the cylinder problem's U0, euler/cylinder/cylinder.cu:26-31)
+ *   SUPERSONIC_VORTEX  supersonic vortex between two arcs about the origin:
+ *                 rho = (1 + A (1 - 1/r^2))^2.5, speed M/r   {M, A}
+ *                 (euler/supersonic/supersonic.cu:26-37; the reference's
+ *                 A = 1.0125 for M = 2.25; A = 0 means (gamma-1)/2 M^2)
+ *   THREEPOINT    oblique shock state for atan(x/y) < theta, gas at rest
+ *                 beyond                                 {M, theta in degrees}
+ *                 (euler/threepoint/threepoint.cu:27-54; PI = 3.14159 as there)
  * Lx, Ly > 0 take distances to the nearest periodic image. */
 enum dgx_ic {
     DGX_IC_GAUSSIAN = 0,
     DGX_IC_POLY = 1,
     DGX_IC_DENSITY_WAVE = 2,
     DGX_IC_VORTEX = 3,
-    DGX_IC_CONSTANT = 4
+    DGX_IC_CONSTANT = 4,
+    DGX_IC_CYLINDER = 5,
+    DGX_IC_SUPERSONIC_VORTEX = 6,
+    DGX_IC_THREEPOINT = 7
 };
 
 typedef struct dgx_mesh dgx_mesh;
@@ -165,13 +181,15 @@ int dgx_set_dt(dgx_solver *solver, int dt_mode, double dt, double cfl);
 /* End time: the last step is clipped to land on it (time_integrator.cu:263-270);
  * t_end <= 0 disables clipping. */
 int dgx_set_end_time(dgx_solver *solver, double t_end);
-/* One RK stage s = 0..3 of the classic RK4 on the resident state
- * (rk_tempstorage / rk4, time_integrator.cu:194-218); stage 0 also fixes dt. */
+/* One stage of the solver's integrator on the resident state: s = 0..3 for RK4
+ * (rk_tempstorage / rk4, time_integrator.cu:194-218), 0..1 for RK2
+ * (rk2_tempstorage / rk2, :445-464), 0 for FE (eval_rhs_fe, :622-700); stage 0
+ * also fixes dt.  Other stage numbers return DGX_ERR_INVALID. */
 int dgx_rk_stage(dgx_solver *solver, int stage, void *stream);
-/* One full time step (CFL + four stages), asynchronous on `stream`. */
+/* One full time step (CFL + every stage), asynchronous on `stream`. */
 int dgx_step(dgx_solver *solver, void *stream);
-/* Advance until t_end or max_steps steps (time_integrate_rk4,
- * time_integrator.cu:221-434); synchronous. */
+/* Advance until t_end or max_steps steps (time_integrate_rk4 / _rk2 / _fe,
+ * time_integrator.cu:221-749); synchronous. */
 int dgx_run(dgx_solver *solver, double t_end, int max_steps, int *steps, double *t,
             void *stream);
 /* Current simulation time and last dt (synchronises the stream). */
@@ -212,15 +230,41 @@ int dgx_write_vertex_values(dgx_solver *solver, const char *path_pattern);
  *   Euler, -2 outflow / -3 inflow: DGX_BC_FREESTREAM params {rho, u, v, p}
  *     (the problem hooks U_outflow / U_inflow, euler.cu:177-241);
  *   advection, any tag: DGX_BC_EXACT, the initial condition `ic` with `params`
- *     translated by a*t (the reference's boundary_exact, 2dadvec_kernels.cu:184-186).
+ *     translated by a*t (the reference's boundary_exact, 2dadvec_kernels.cu:184-186);
+ *   Euler, DGX_BC_PROBLEM with ic = CYLINDER / SUPERSONIC_VORTEX / THREEPOINT and
+ *     that initial condition's params: the problem file's own hooks for all
+ *     three tags --
+ *       cylinder: -1 momentum reduced to its part tangential to the circle
+ *         about (0.5, 0.5) through the point, -2/-3 the free stream
+ *         (cylinder.cu:38-111);
+ *       supersonic vortex: -1 the same about the origin, -2/-3 the vortex
+ *         state at the point (supersonic.cu:40-113);
+ *       three-point: -1 flips the x momentum where m.n > 0, else the y
+ *         momentum, -2 the shock state, -3 the shock state left of the front
+ *         x = M t cos(theta) + tan(theta), else the initial state
+ *         (threepoint.cu:56-109).
+ *     The reference's radial reflections take the point with side 1's two
+ *     reference coordinates exchanged (cylinder.cu:78-81, supersonic.cu:86-89);
+ *     kept alike.
  * Without a setting, outflow/inflow and advection sides take the interior state. */
-enum dgx_bc { DGX_BC_NONE = 0, DGX_BC_FREESTREAM = 1, DGX_BC_EXACT = 2 };
+enum dgx_bc { DGX_BC_NONE = 0, DGX_BC_FREESTREAM = 1, DGX_BC_EXACT = 2, DGX_BC_PROBLEM = 3 };
 int dgx_solver_set_boundary(dgx_solver *solver, int kind, int ic, const double *params);
 /* Kernel options of a solver (for autotuning and tests):
  *   DGX_OPT_PREFETCH  1 (default): RK stages 2-4 copy the tile's base state and
  *                     accumulator into shared memory with the TMA engine while
  *                     the element work runs; 0: plain loads at the end. */
-enum dgx_option { DGX_OPT_PREFETCH = 1 };
+/*   DGX_OPT_STAGE_TIME  the time at which a stage evaluates time-dependent
+ *                     boundary data:
+ *                     DGX_STAGE_TIME_EXACT (default) t_n + c_s dt with the
+ *                       integrator's nodes c_s (RK4 0, 1/2, 1/2, 1; RK2 0, 1/2);
+ *                     DGX_STAGE_TIME_REFERENCE the reference's arguments: Euler
+ *                       RK4/RK2 pass t_{n+1} + c_s dt (time_integrator.cu:264-380,
+ *                       :509-561), Euler FE and every advection stage pass t_n
+ *                       (time_integrator.cu:733, src/2d/time_integrator.cu:145).
+ *                     Periodic meshes and time-independent boundary data give
+ *                     the same results under both. */
+enum dgx_option { DGX_OPT_PREFETCH = 1, DGX_OPT_STAGE_TIME = 2 };
+enum dgx_stage_time { DGX_STAGE_TIME_EXACT = 0, DGX_STAGE_TIME_REFERENCE = 1 };
 int dgx_solver_set_option(dgx_solver *solver, int option, int value);
 /* Number of CUDA kernels this solver has launched so far. */
 int dgx_launch_count(const dgx_solver *solver, long long *count);
@@ -233,8 +277,8 @@ int dgx_launch_count(const dgx_solver *solver, long long *count);
  * batched kernel computes every solve's dt, and the whole step is captured as
  * a CUDA graph.  Every solve keeps its own state, time, dt rule and end time
  * (set them before creating the batch); each solve's result equals the same
- * solve run alone with dgx_step, bit for bit.  Destroy the batch before its
- * solvers. */
+ * solve run alone with dgx_step, bit for bit.  Batches take RK4 solvers only
+ * (others: DGX_ERR_UNSUPPORTED).  Destroy the batch before its solvers. */
 typedef struct dgx_batch dgx_batch;
 int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out);
 int dgx_batch_destroy(dgx_batch *batch);

@@ -293,10 +293,35 @@ typedef struct {
     double min_diam;
     /* boundary ghost states: 0 none (interior state), 1 free-stream state
      * (Euler inflow/outflow), 2 exact initial condition translated by a*t
-     * (advection) */
+     * (advection), 3 a problem's own ghost states (bc_ic = its IC) */
     int bc_kind, bc_ic;
+    int integrator;       /* 0 RK4, 1 RK2 midpoint, 2 forward Euler */
+    int ref_time;         /* 1: the reference's stage-time arguments */
     double bc_state[4], bc_params[8];
 } orc_solver;
+
+enum {
+    ORC_IC_GAUSSIAN = 0,      /* u = exp(-((x-x0)^2 + (y-y0)^2) / w)          params x0 y0 w [Lx Ly] */
+    ORC_IC_POLY = 1,          /* u = (x - y)^alpha                             params alpha */
+    ORC_IC_DENSITY_WAVE = 2,  /* rho = 1 + A sin(2 pi k (x+y)), u, v, p const  params A u v p k */
+    ORC_IC_VORTEX = 3,        /* isentropic vortex                             params x0 y0 beta uinf vinf Lx Ly */
+    ORC_IC_CONSTANT = 4,      /* constant state                                params rho u v p (or u) */
+    ORC_IC_CYLINDER = 5,      /* free stream rho = gamma, u = M, p = 1         params M */
+    ORC_IC_SUPERSONIC = 6,    /* supersonic vortex between two arcs            params M A */
+    ORC_IC_THREEPOINT = 7,    /* oblique shock state inside the angle theta    params M theta_deg */
+};
+
+/* the reference's problem files define PI as 3.14159 (threepoint.cu:13) */
+#define ORC_REF_PI 3.14159
+
+/* oblique shock state of the three-point problem (U_shock, threepoint.cu:27-32) */
+static void orc_threepoint_shock(const double *P, double g, double *U) {
+    double a = P[1] * ORC_REF_PI / 180.;
+    U[0] = g;
+    U[1] = P[0] * cos(a) * U[0];
+    U[2] = P[0] * sin(a) * U[0];
+    U[3] = 0.5 * U[0] * P[0] * P[0] + 1. / (g - 1.0);
+}
 
 void orc_ic_eval(int ic, const double *P, double g, double x, double y, double *U);
 
@@ -478,9 +503,70 @@ static void orc_phys_flux(const orc_solver *S, const double *U, double *fx, doub
  * euler.cu:177-241) or the interior state; advection takes the initial
  * condition translated by a*t (boundary_exact, 2dadvec_kernels.cu:184-186) or
  * the interior state. */
+/* point j of local side ls of element L (the mapping of inflow_boundary,
+ * euler.cu:186-205) */
+static void orc_side_xy(const orc_solver *S, int L, int ls, int j, double *x, double *y) {
+    const orc_tables *T = &S->T;
+    double g = T->s1[j], gr = T->s1[T->nq1 - 1 - j], r, s;
+    if (ls == 0) { r = 0.5 + 0.5 * g; s = 0.0; }
+    else if (ls == 1) { r = (1.0 - g) / 2.0; s = (1.0 + g) / 2.0; }
+    else { r = 0.0; s = 0.5 + 0.5 * gr; }
+    *x = S->V[0][L] + S->xr[L] * r + S->xs[L] * s;
+    *y = S->V[1][L] + S->yr[L] * r + S->ys[L] * s;
+}
+
+/* Problem ghost states (DGX_BC_PROBLEM), the reference's problem hooks:
+ *   cylinder    -1 tangential momentum about the radial direction from (0.5, 0.5)
+ *                  (reflecting_boundary, cylinder.cu:58-111); -2/-3 the free stream
+ *   supersonic  -1 the same about the origin (supersonic.cu:66-113); -2/-3 U0(x, y)
+ *   three-point -1 flips the normal-facing momentum component (threepoint.cu:86-109);
+ *               -2 the shock state; -3 the shock state left of the moving front
+ *                  x < M t cos(theta) + tan(theta), else U0 (threepoint.cu:60-76)
+ * The reference's radial reflections take their point from the mapping with
+ * side 1's two coordinates exchanged (cylinder.cu:78-81), i.e. point
+ * n_quad1d-1-j of side 1; kept alike. */
+static void orc_problem_ghost(const orc_solver *S, int tag, int L, int ls, int j, double t,
+                              const double *UL, double nx, double ny, double *UR) {
+    const double *P = S->bc_params;
+    double x, y;
+    if (S->bc_ic == ORC_IC_THREEPOINT) {
+        if (tag == -1) {
+            UR[0] = UL[0]; UR[3] = UL[3];
+            if ((float)(UL[1] * nx + UL[2] * ny) > 0.f) { UR[1] = -UL[1]; UR[2] = UL[2]; }
+            else { UR[1] = UL[1]; UR[2] = -UL[2]; }
+        } else if (tag == -2) {
+            orc_threepoint_shock(P, S->gamma, UR);
+        } else {
+            double a = P[1] * ORC_REF_PI / 180.;
+            orc_side_xy(S, L, ls, j, &x, &y);
+            if (x < P[0] * t * cos(a) + tan(a)) orc_threepoint_shock(P, S->gamma, UR);
+            else orc_ic_eval(ORC_IC_THREEPOINT, P, S->gamma, x, y, UR);
+        }
+        return;
+    }
+    if (tag == -1) {
+        double cx = S->bc_ic == ORC_IC_CYLINDER ? 0.5 : 0.0, cy = cx, d, Nx, Ny, tm;
+        orc_side_xy(S, L, ls, ls == 1 ? S->T.nq1 - 1 - j : j, &x, &y);
+        x -= cx; y -= cy;
+        d = sqrt(x * x + y * y);
+        Nx = x / d; Ny = y / d;
+        tm = UL[1] * Ny - UL[2] * Nx;
+        UR[0] = UL[0]; UR[3] = UL[3];
+        UR[1] = tm * Ny;
+        UR[2] = -tm * Nx;
+        return;
+    }
+    orc_side_xy(S, L, ls, j, &x, &y);
+    orc_ic_eval(S->bc_ic, P, S->gamma, x, y, UR);
+}
+
 static void orc_ghost(const orc_solver *S, int tag, int L, int ls, int j, double t, const double *UL,
                       double nx, double ny, double *UR) {
     int n;
+    if (S->eq == ORC_EULER && S->bc_kind == 3) {
+        orc_problem_ghost(S, tag, L, ls, j, t, UL, nx, ny, UR);
+        return;
+    }
     if (S->eq == ORC_EULER) {
         if (tag == -1) {
             double mn = UL[1] * nx + UL[2] * ny;
@@ -491,13 +577,8 @@ static void orc_ghost(const orc_solver *S, int tag, int L, int ls, int j, double
             for (n = 0; n < 4; n++) UR[n] = UL[n];
         }
     } else if (S->bc_kind == 2) {
-        const orc_tables *T = &S->T;
-        double g = T->s1[j], gr = T->s1[T->nq1 - 1 - j], r, s, x, y, U[4];
-        if (ls == 0) { r = 0.5 + 0.5 * g; s = 0.0; }
-        else if (ls == 1) { r = (1.0 - g) / 2.0; s = (1.0 + g) / 2.0; }
-        else { r = 0.0; s = 0.5 + 0.5 * gr; }
-        x = S->V[0][L] + S->xr[L] * r + S->xs[L] * s;
-        y = S->V[1][L] + S->yr[L] * r + S->ys[L] * s;
+        double x, y, U[4];
+        orc_side_xy(S, L, ls, j, &x, &y);
         orc_ic_eval(S->bc_ic, S->bc_params, S->gamma, x - S->ax * t, y - S->ay * t, U);
         UR[0] = U[0];
     } else {
@@ -511,7 +592,8 @@ int orc_set_boundary(orc_solver *S, int kind, int ic, const double *params) {
         double rho = params[0], u = params[1], v = params[2], p = params[3];
         S->bc_state[0] = rho; S->bc_state[1] = rho * u; S->bc_state[2] = rho * v;
         S->bc_state[3] = p / (S->gamma - 1.0) + 0.5 * rho * (u * u + v * v);
-    } else if (kind == 2) {
+    } else if (kind == 2 || kind == 3) {
+        if (kind == 3 && (ic < ORC_IC_CYLINDER || ic > ORC_IC_THREEPOINT)) return -1;
         S->bc_ic = ic;
         for (i = 0; i < 8; i++) S->bc_params[i] = params ? params[i] : 0.0;
     }
@@ -627,6 +709,24 @@ double orc_cfl_dt(const orc_solver *S, const double *c, double cfl) {
     return cfl * S->min_diam / orc_max_lambda(S, c) / (2. * S->T.p + 1.);
 }
 
+/* Time integrator and stage-time rule.  Stage s of a step from t_n takes its
+ * boundary data at t_n + c_s dt; with ref_time the reference's arguments
+ * instead: Euler RK4/RK2 pass t_{n+1} + c_s dt (time_integrator.cu:264-380,
+ * :509-561), Euler forward Euler and every advection stage pass t_n
+ * (time_integrator.cu:733; src/2d/time_integrator.cu:145). */
+int orc_set_integrator(orc_solver *S, int integrator, int ref_time) {
+    if (integrator < 0 || integrator > 2) return -1;
+    S->integrator = integrator;
+    S->ref_time = ref_time ? 1 : 0;
+    return 0;
+}
+
+static double orc_stage_time(const orc_solver *S, double t, double dt, double node) {
+    if (!S->ref_time) return t + node * dt;
+    if (S->eq == ORC_EULER && S->integrator != 2) return (t + dt) + node * dt;
+    return t;
+}
+
 /* one classic RK4 step in the reference's form (time_integrator.cu:276-398) */
 int orc_rk4_step(orc_solver *S, double *c, double dt, double t) {
     size_t N = (size_t)S->nv * S->T.np * S->num_elem, i;
@@ -635,7 +735,7 @@ int orc_rk4_step(orc_solver *S, double *c, double dt, double t) {
     int st, rc;
     const double *src = c;
     for (st = 0; st < 4; st++) {
-        rc = orc_rhs(S, src, S->k[st], dt, t + tfrac[st] * dt);
+        rc = orc_rhs(S, src, S->k[st], dt, orc_stage_time(S, t, dt, tfrac[st]));
         if (rc) return rc;
         if (st < 3) {
             double a = alpha[st];
@@ -653,6 +753,49 @@ int orc_rk4_step(orc_solver *S, double *c, double dt, double t) {
     return 0;
 }
 
+/* one explicit-midpoint step: k1 = k(c), k* = c + k1/2, c += k(k*)
+ * (rk2_tempstorage / rk2 in time_integrate_rk2, time_integrator.cu:445-464,
+ * 518-580) */
+int orc_rk2_step(orc_solver *S, double *c, double dt, double t) {
+    size_t N = (size_t)S->nv * S->T.np * S->num_elem, i;
+    int rc = orc_rhs(S, c, S->k[0], dt, orc_stage_time(S, t, dt, 0.0));
+    if (rc) return rc;
+    {
+        double *ks = S->kstar, *k1 = S->k[0];
+#pragma omp parallel for schedule(static)
+        for (i = 0; i < N; i++) ks[i] = c[i] + 0.5 * k1[i];
+    }
+    rc = orc_rhs(S, S->kstar, S->k[1], dt, orc_stage_time(S, t, dt, 0.5));
+    if (rc) return rc;
+    {
+        double *k2 = S->k[1];
+#pragma omp parallel for schedule(static)
+        for (i = 0; i < N; i++) c[i] += k2[i];
+    }
+    return 0;
+}
+
+/* one forward-Euler step: c += dt/J (volume + surface) (eval_rhs_fe,
+ * time_integrator.cu:622-700) */
+int orc_fe_step(orc_solver *S, double *c, double dt, double t) {
+    size_t N = (size_t)S->nv * S->T.np * S->num_elem, i;
+    int rc = orc_rhs(S, c, S->k[0], dt, orc_stage_time(S, t, dt, 0.0));
+    if (rc) return rc;
+    {
+        double *k1 = S->k[0];
+#pragma omp parallel for schedule(static)
+        for (i = 0; i < N; i++) c[i] += k1[i];
+    }
+    return 0;
+}
+
+/* one step of the solver's integrator from time t */
+int orc_step(orc_solver *S, double *c, double dt, double t) {
+    if (S->integrator == 1) return orc_rk2_step(S, c, dt, t);
+    if (S->integrator == 2) return orc_fe_step(S, c, dt, t);
+    return orc_rk4_step(S, c, dt, t);
+}
+
 /* Run to t_end (dt_mode 0: fixed dt, 1: reference CFL rule with factor `cfl`),
  * clipping the last step to land on t_end (time_integrator.cu:263-270), or at
  * most max_steps steps when max_steps > 0.  Returns the number of steps. */
@@ -665,7 +808,7 @@ int orc_run(orc_solver *S, double *c, int dt_mode, double dt_fixed, double cfl, 
         double t0 = t;
         if (t + dt > t_end) { dt = t_end - t; t = t_end; }
         else t += dt;
-        rc = orc_rk4_step(S, c, dt, t0);
+        rc = orc_step(S, c, dt, t0);
         if (rc) return rc;
         steps++;
     }
@@ -677,13 +820,6 @@ int orc_run(orc_solver *S, double *c, int dt_mode, double dt_fixed, double cfl, 
 /* Initial conditions: L2 projection with the degree-2p rule (no mass solve,  */
 /* the basis is orthonormal on the reference triangle)                        */
 /* ------------------------------------------------------------------------- */
-enum {
-    ORC_IC_GAUSSIAN = 0,      /* u = exp(-((x-x0)^2 + (y-y0)^2) / w)          params x0 y0 w [Lx Ly] */
-    ORC_IC_POLY = 1,          /* u = (x - y)^alpha                             params alpha */
-    ORC_IC_DENSITY_WAVE = 2,  /* rho = 1 + A sin(2 pi k (x+y)), u, v, p const  params A u v p k */
-    ORC_IC_VORTEX = 3,        /* isentropic vortex                             params x0 y0 beta uinf vinf Lx Ly */
-    ORC_IC_CONSTANT = 4,      /* constant state                                params rho u v p (or u) */
-};
 
 static double orc_wrap(double d, double L) {
     if (L > 0) { d = fmod(d, L); if (d > 0.5 * L) d -= L; if (d < -0.5 * L) d += L; }
@@ -714,6 +850,31 @@ void orc_ic_eval(int ic, const double *P, double g, double x, double y, double *
         double rho = pow(T, 1.0 / (g - 1.0)), p = pow(rho, g);
         double u = P[3] + du, v = P[4] + dv;
         U[0] = rho; U[1] = rho * u; U[2] = rho * v; U[3] = p / (g - 1.0) + 0.5 * rho * (u * u + v * v);
+        break;
+    }
+    case ORC_IC_CYLINDER:   /* U0, cylinder.cu:26-31 */
+        U[0] = g; U[1] = U[0] * P[0]; U[2] = 0.0;
+        U[3] = 0.5 * U[0] * P[0] * P[0] + 1. / (g - 1.0);
+        break;
+    case ORC_IC_SUPERSONIC: {   /* U0, supersonic.cu:26-37 (powf there, pow here) */
+        double r = sqrt(x * x + y * y), th = atan(y / x);
+        double A = P[1] != 0.0 ? P[1] : 0.5 * (g - 1.0) * P[0] * P[0];
+        double p;
+        U[0] = pow(1 + A * (1. - 1. / (r * r)), 2.5);
+        U[1] = U[0] * sin(th) * P[0] / r;
+        U[2] = U[0] * -cos(th) * P[0] / r;
+        p = (1.0 / g) * pow(U[0], g);
+        U[3] = 0.5 * U[0] * (P[0] * P[0] / (r * r)) + p * (1. / (g - 1.));
+        break;
+    }
+    case ORC_IC_THREEPOINT: {   /* U0, threepoint.cu:44-54 */
+        double angle = atan(x / y);
+        if (angle < P[1] * ORC_REF_PI / 180) {
+            orc_threepoint_shock(P, g, U);
+        } else {
+            U[0] = 0.5 * g; U[1] = 0.; U[2] = 0.;
+            U[3] = 0.5 * U[0] * P[0] * P[0] + 1. / (g - 1.0);
+        }
         break;
     }
     case ORC_IC_CONSTANT:

@@ -19,6 +19,7 @@ REF_BIN = os.path.join(HERE, "_ref", "ref_euler")
 ADVECTION, EULER = 0, 1
 CENTRAL, LLF = 0, 1
 IC_GAUSSIAN, IC_POLY, IC_DENSITY_WAVE, IC_VORTEX, IC_CONSTANT = 0, 1, 2, 3, 4
+RK4, RK2, FE = 0, 1, 2
 
 _lib = None
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -62,6 +63,8 @@ def lib():
         L.orc_cfl_dt.argtypes = [C.c_void_p, _dp, C.c_double]
         L.orc_cfl_dt.restype = C.c_double
         L.orc_rk4_step.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
+        L.orc_step.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
+        L.orc_set_integrator.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.orc_run.argtypes = [C.c_void_p, _dp, C.c_int, C.c_double, C.c_double, C.c_double,
                               C.c_int, C.POINTER(C.c_double)]
         L.orc_totals.argtypes = [C.c_void_p, _dp, _dp]
@@ -161,6 +164,12 @@ class Oracle:
         P[:len(params)] = params
         lib().orc_set_boundary(self.h, int(kind), int(ic), P)
 
+    def set_integrator(self, integrator: int, reference_stage_time: bool = False) -> None:
+        """RK4 (default), RK2 midpoint or FE; reference_stage_time selects the
+        reference's stage-time arguments for time-dependent boundary data."""
+        if lib().orc_set_integrator(self.h, int(integrator), int(bool(reference_stage_time))):
+            raise ValueError(f"unknown integrator {integrator}")
+
     def max_lambda(self, c) -> float:
         return lib().orc_max_lambda(self.h, self._state(c))
 
@@ -169,9 +178,9 @@ class Oracle:
 
     def step(self, c, dt: float, t: float = 0.0) -> np.ndarray:
         c = self._state(c).copy()
-        rc = lib().orc_rk4_step(self.h, c, dt, t)
+        rc = lib().orc_step(self.h, c, dt, t)
         if rc:
-            raise RuntimeError(f"orc_rk4_step failed ({rc})")
+            raise RuntimeError(f"orc_step failed ({rc})")
         return c
 
     def run(self, c, t_end: float, dt: float | None = None, cfl: float = 0.7,

@@ -15,9 +15,12 @@
  * (basis.c:150-237), surface (euler_kernels.c:823-984), volume (:986-1104),
  * eval_rhs_rk4 (time_integrator_euler.c:68-136), rk4_tempstorage and rk4
  * (time_integrator_euler.c:19-41) in the order of time_integrate_rk4
- * (time_integrator_euler.c:138-287) with a fixed dt.
+ * (time_integrator_euler.c:138-287) with a fixed dt; then, from the same
+ * initial state, forward-Euler steps through eval_rhs_fe
+ * (time_integrator_euler.c:289-356) in the order of time_integrate_fe
+ * (:359-406), also with a fixed dt.
  *
- * Input file (little-endian): int32[8] {num_elem, num_sides, p, nsteps, 0...},
+ * Input file (little-endian): int32[8] {num_elem, num_sides, p, nsteps, fe_steps, 0...},
  * float64 dt, float64 V1x..V3y[E] (6 arrays), int32 elem_s1..3[E],
  * int32 left_elem, right_elem, left_side, right_side [S], float64 c0[4*Np*E].
  * Output file: see write order in main() below.
@@ -36,7 +39,7 @@ static void xwrite(FILE *f, const void *p, size_t n) {
 
 int main(int argc, char *argv[]) {
     FILE *in, *out;
-    int hdr[8], E, S, n, n_p, nsteps, i, step;
+    int hdr[8], E, S, n, n_p, nsteps, fe_steps, i, step;
     double dt;
     double *V[6];
     int *es[3], *le, *re, *lsn, *rsn;
@@ -49,7 +52,7 @@ int main(int argc, char *argv[]) {
     in = fopen(argv[1], "rb");
     if (!in) return 1;
     if (fread(hdr, sizeof(int), 8, in) != 8) return 2;
-    E = hdr[0]; S = hdr[1]; n = hdr[2]; nsteps = hdr[3];
+    E = hdr[0]; S = hdr[1]; n = hdr[2]; nsteps = hdr[3]; fe_steps = hdr[4];
     n_p = (n + 1) * (n + 2) / 2;
     if (fread(&dt, sizeof(double), 1, in) != 1) return 2;
     for (i = 0; i < 6; i++) V[i] = (double *)xread(in, sizeof(double) * E);
@@ -145,6 +148,20 @@ int main(int argc, char *argv[]) {
         rk4(d_c, d_k1, d_k2, d_k3, d_k4, n_p, E);
     }
     xwrite(out, d_c, sizeof(double) * NV);
+
+    /* fe_steps forward-Euler steps from the initial state */
+    if (fe_steps > 0) {
+        memcpy(d_c, c0, sizeof(double) * NV);
+        for (step = 0; step < fe_steps; step++) {
+            eval_surface(d_c, d_left_riemann_rhs, d_right_riemann_rhs, d_s_length, d_V1x, d_V1y,
+                         d_V2x, d_V2y, d_V3x, d_V3y, d_left_elem, d_right_elem, d_left_side_number,
+                         d_right_side_number, d_Nx, d_Ny, n_quad1d, n_quad, n_p, S, E, 0.0);
+            eval_volume(d_c, d_quad_rhs, d_xr, d_yr, d_xs, d_ys, n_quad, n_p, E);
+            eval_rhs_fe(d_c, d_quad_rhs, d_left_riemann_rhs, d_right_riemann_rhs, d_elem_s1,
+                        d_elem_s2, d_elem_s3, d_left_elem, d_J, dt, n_p, S, E);
+        }
+        xwrite(out, d_c, sizeof(double) * NV);
+    }
     fclose(out);
     return 0;
 }

@@ -5,7 +5,8 @@ reference's src/2d/conservation/euler/cpu sources by ``make -C oracle ref``) on
 small seeded periodic meshes and stores, per case, the inputs (mesh arrays,
 order, initial coefficients, dt, step count) and the reference's outputs:
 basis and quadrature tables, geometric factors, cell wave speeds, one RHS
-evaluation with dt = 1 and the state after a few fixed-dt RK4 steps.
+evaluation with dt = 1, the state after a few fixed-dt RK4 steps and the state
+after as many forward-Euler steps from the same start.
 
 Needs the reference tree, so it runs only where the reference is mounted:
 
@@ -62,7 +63,8 @@ def run_case(ref_bin, name, build, p, ic, params, dt, nsteps):
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
-            np.array([E, S, p, nsteps, 0, 0, 0, 0], dtype=np.int32).tofile(f)
+            # nsteps RK4 steps, then as many forward-Euler steps from c0
+            np.array([E, S, p, nsteps, nsteps, 0, 0, 0], dtype=np.int32).tofile(f)
             np.array([dt], dtype=np.float64).tofile(f)
             for a in mesh.vertices():
                 a.astype(np.float64).tofile(f)
@@ -95,6 +97,7 @@ def run_case(ref_bin, name, build, p, ic, params, dt, nsteps):
     take("lambda", E)
     take("rhs", 4 * np_ * E, (4, np_, E))
     take("c_final", 4 * np_ * E, (4, np_, E))
+    take("c_fe", 4 * np_ * E, (4, np_, E))
     assert off == len(raw)
     arrays = dict(
         p=np.int32(p), nsteps=np.int32(nsteps), dt=np.float64(dt), ic=np.int32(ic),

@@ -58,3 +58,17 @@ def test_oracle_matches_reference(path, oracle_mod):
     assert orc.rel_l2(o64.rhs(z["c0"], 1.0), z["ref_rhs"]).max() <= max(1e-7, RHS_TOL[p])
     lam = o64.max_lambda(z["c0"])
     assert abs(lam - z["ref_lambda"].max()) <= 1e-6 * lam
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_forward_euler_matches_reference(path, oracle_mod):
+    """Forward-Euler steps against the reference's eval_rhs_fe loop."""
+    orc = oracle_mod
+    z, m = load(path)
+    p = int(z["p"])
+    o = orc.Oracle(m, p, orc.EULER, orc.LLF, 1.4, ref_sqrtf=True)
+    o.set_integrator(orc.FE)
+    c = z["c0"].copy()
+    for _ in range(int(z["nsteps"])):
+        c = o.step(c, float(z["dt"]))
+    assert orc.rel_l2(c, z["ref_c_fe"]).max() <= RHS_TOL[p] * 1e-2
