@@ -25,8 +25,10 @@ int ensure_device_tables() {
     if (dev < 0 || dev >= 64) { set_error("device index %d out of range", dev); return DGX_ERR_UNSUPPORTED; }
     std::lock_guard<std::mutex> lk(g_init_mu);
     if (g_tables_ready[dev]) return DGX_OK;
-    int rc = upload_tables_f32();
-    if (!rc) rc = upload_tables_f64();
+    int rc = upload_tables_f32_nb();
+    if (!rc) rc = upload_tables_f32_b();
+    if (!rc) rc = upload_tables_f64_nb();
+    if (!rc) rc = upload_tables_f64_b();
     if (!rc) rc = upload_tables_misc();
     if (!rc) g_tables_ready[dev] = true;
     return rc;
@@ -101,8 +103,7 @@ size_t elem_size(const SolverDev &s) { return s.precision == DGX_FP64 ? sizeof(d
 int stage_launch(dgx_solver *sv, int mode, const void *u, const void *c, void *acc, void *out,
                  double dt, double t, cudaStream_t st) {
     const StageArgs a = make_stage_args(sv, mode, u, c, acc, out, dt, t);
-    const int rc = sv->s.precision == DGX_FP64 ? launch_stage_f64(sv->s.order, sv->s.equation, a, st)
-                                               : launch_stage_f32(sv->s.order, sv->s.equation, a, st);
+    const int rc = launch_stage(sv->s.precision, sv->s.order, sv->s.equation, a, st);
     if (!rc) sv->launches++;
     return rc;
 }
@@ -191,8 +192,8 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
     a.bc_ic = s.bc_ic;
     for (int i = 0; i < 4; ++i) a.bc_state[i] = s.bc_state[i];
     for (int i = 0; i < 8; ++i) a.bc_params[i] = s.bc_params[i];
-    a.vx1 = m.V;
-    a.vy1 = m.V + m.num_elem;
+    a.V = m.V;
+    a.bnd = m.num_boundary > 0 ? 1 : 0;
     if (s.precision == DGX_FP64) {
         a.geo = m.geo64;
         a.fn = m.fn64;

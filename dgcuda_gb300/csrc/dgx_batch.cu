@@ -22,6 +22,7 @@ namespace {
 
 struct BatchClass {
     int precision = 0, order = 0, equation = 0;
+    int bnd = 0;                             // the class's meshes have boundary sides
     std::vector<int> solves;                 // indices into the batch's solver list
     StageArgs *d_args[4] = {nullptr, nullptr, nullptr, nullptr};
     int2 *d_items = nullptr;
@@ -80,10 +81,10 @@ int class_launch(dgx_batch *b, BatchClass &k, int stage, cudaStream_t st) {
     a.n_items = k.n_items;
     a.nslot = k.nslot;
     a.prefetch = stage >= 1 ? k.prefetch : 0;
+    a.bnd = k.bnd;
     if (k.persistent > 0) a.grid = std::min(k.n_items, num_sms() * k.persistent);
     else a.grid = k.n_items;
-    const int rc = k.precision == DGX_FP64 ? launch_batch_stage_f64(k.order, k.equation, a, st)
-                                           : launch_batch_stage_f32(k.order, k.equation, a, st);
+    const int rc = launch_batch_stage(k.precision, k.order, k.equation, a, st);
     if (!rc && a.grid > 0) b->launches++;
     return rc;
 }
@@ -119,9 +120,8 @@ int class_upload(dgx_batch *b, BatchClass &k) {
         return class_upload(b, k);
     }
     // set the kernel's shared-memory limit outside any capture (grid 0: no launch)
-    BatchStageArgs probe{k.d_args[1], k.d_items, 0, 0, k.nslot, k.prefetch};
-    int rc = k.precision == DGX_FP64 ? launch_batch_stage_f64(k.order, k.equation, probe, nullptr)
-                                     : launch_batch_stage_f32(k.order, k.equation, probe, nullptr);
+    BatchStageArgs probe{k.d_args[1], k.d_items, 0, 0, k.nslot, k.prefetch, k.bnd};
+    int rc = launch_batch_stage(k.precision, k.order, k.equation, probe, nullptr);
     return rc;
 }
 
@@ -231,14 +231,16 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
     for (int i = 0; i < n; ++i) {
         const SolverDev &s = solvers[i]->s;
         BatchClass *k = nullptr;
+        const int bnd = solvers[i]->mesh->d.num_boundary > 0 ? 1 : 0;
         for (auto &c : b->classes)
-            if (c.precision == s.precision && c.order == s.order && c.equation == s.equation) k = &c;
+            if (c.precision == s.precision && c.order == s.order && c.equation == s.equation && c.bnd == bnd) k = &c;
         if (!k) {
             b->classes.emplace_back();
             k = &b->classes.back();
             k->precision = s.precision;
             k->order = s.order;
             k->equation = s.equation;
+            k->bnd = bnd;
         }
         k->solves.push_back(i);
         k->dofs += static_cast<long long>(s.n);

@@ -15,6 +15,19 @@ __device__ inline double wrap_dist(double d, double L) {
     return d;
 }
 
+// the reference's problem files define PI as 3.14159 (threepoint.cu:13)
+constexpr double kRefPi = 3.14159;
+
+// oblique shock state of the three-point problem (U_shock, threepoint.cu:27-32):
+// P = {M, theta in degrees}
+__device__ inline void threepoint_shock(const double *P, double g, double *U) {
+    const double a = P[1] * kRefPi / 180.0;
+    U[0] = g;
+    U[1] = P[0] * cos(a) * U[0];
+    U[2] = P[0] * sin(a) * U[0];
+    U[3] = 0.5 * U[0] * P[0] * P[0] + 1.0 / (g - 1.0);
+}
+
 __device__ inline void ic_eval(int ic, const double *P, double g, double x, double y, double *U) {
     const double pi = 3.14159265358979323846;
     switch (ic) {
@@ -42,6 +55,28 @@ __device__ inline void ic_eval(int ic, const double *P, double g, double x, doub
         U[3] = p / (g - 1.0) + 0.5 * rho * (u * u + v * v);
         break;
     }
+    case DGX_IC_CYLINDER:   // free stream of the cylinder problem (cylinder.cu:26-31)
+        U[0] = g; U[1] = U[0] * P[0]; U[2] = 0.0;
+        U[3] = 0.5 * U[0] * P[0] * P[0] + 1.0 / (g - 1.0);
+        break;
+    case DGX_IC_SUPERSONIC_VORTEX: {   // supersonic.cu:28-38 (pow for its powf)
+        const double r = sqrt(x * x + y * y), th = atan(y / x);
+        const double A = P[1] != 0.0 ? P[1] : 0.5 * (g - 1.0) * P[0] * P[0];
+        U[0] = pow(1.0 + A * (1.0 - 1.0 / (r * r)), 2.5);
+        U[1] = U[0] * sin(th) * P[0] / r;
+        U[2] = U[0] * -cos(th) * P[0] / r;
+        const double p = (1.0 / g) * pow(U[0], g);
+        U[3] = 0.5 * U[0] * (P[0] * P[0] / (r * r)) + p * (1.0 / (g - 1.0));
+        break;
+    }
+    case DGX_IC_THREEPOINT:   // threepoint.cu:44-54
+        if (atan(x / y) < P[1] * kRefPi / 180.0) {
+            threepoint_shock(P, g, U);
+        } else {
+            U[0] = 0.5 * g; U[1] = 0.0; U[2] = 0.0;
+            U[3] = 0.5 * U[0] * P[0] * P[0] + 1.0 / (g - 1.0);
+        }
+        break;
     default:
         U[0] = P[0]; U[1] = P[0] * P[1]; U[2] = P[0] * P[2];
         U[3] = P[3] / (g - 1.0) + 0.5 * P[0] * (P[1] * P[1] + P[2] * P[2]);

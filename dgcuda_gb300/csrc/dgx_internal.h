@@ -122,8 +122,12 @@ struct dgx_solver {
 namespace dgx {
 
 // kernels/launchers implemented in the .cu sources
-int upload_tables_f32();
-int upload_tables_f64();
+// each stage translation unit (precision x with/without boundary sides) owns
+// its constant tables
+int upload_tables_f32_nb();
+int upload_tables_f32_b();
+int upload_tables_f64_nb();
+int upload_tables_f64_b();
 int upload_tables_misc();
 
 struct StageArgs {
@@ -154,7 +158,8 @@ struct StageArgs {
     int bc_kind, bc_ic;
     double bc_state[4];
     double bc_params[8];
-    const double *vx1, *vy1;   // first vertex of every element (FP64)
+    const double *V;           // element vertices V1x, V1y, V2x, V2y, V3x, V3y [6][E] (FP64)
+    int bnd;                   // the mesh has boundary sides (selects the kernels with ghost states)
 };
 
 // Batched launch: items[i] = (index into args, tile); grid CTAs walk the list.
@@ -165,14 +170,31 @@ struct BatchStageArgs {
     int grid;
     int nslot;               // largest nslot of the class (shared-memory size)
     int prefetch;            // any solve of the class prefetches
+    int bnd;                 // any solve of the class has boundary sides
 };
 
-int launch_stage_f32(int order, int equation, const StageArgs &a, cudaStream_t st);
-int launch_batch_stage_f32(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
-int launch_batch_stage_f64(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
+// _nb: kernels without ghost-state code (meshes without boundary sides); _b: with it
+int launch_stage_f32_nb(int order, int equation, const StageArgs &a, cudaStream_t st);
+int launch_stage_f32_b(int order, int equation, const StageArgs &a, cudaStream_t st);
+int launch_stage_f64_nb(int order, int equation, const StageArgs &a, cudaStream_t st);
+int launch_stage_f64_b(int order, int equation, const StageArgs &a, cudaStream_t st);
+int launch_batch_stage_f32_nb(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
+int launch_batch_stage_f32_b(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
+int launch_batch_stage_f64_nb(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
+int launch_batch_stage_f64_b(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
 size_t batch_smem_f32(int order, int equation, int nslot, int prefetch);
 size_t batch_smem_f64(int order, int equation, int nslot, int prefetch);
-int launch_stage_f64(int order, int equation, const StageArgs &a, cudaStream_t st);
+inline int launch_stage(int precision, int order, int equation, const StageArgs &a, cudaStream_t st) {
+    if (precision == DGX_FP64)
+        return a.bnd ? launch_stage_f64_b(order, equation, a, st) : launch_stage_f64_nb(order, equation, a, st);
+    return a.bnd ? launch_stage_f32_b(order, equation, a, st) : launch_stage_f32_nb(order, equation, a, st);
+}
+inline int launch_batch_stage(int precision, int order, int equation, const BatchStageArgs &b, cudaStream_t st) {
+    if (precision == DGX_FP64)
+        return b.bnd ? launch_batch_stage_f64_b(order, equation, b, st)
+                     : launch_batch_stage_f64_nb(order, equation, b, st);
+    return b.bnd ? launch_batch_stage_f32_b(order, equation, b, st) : launch_batch_stage_f32_nb(order, equation, b, st);
+}
 
 // per-solve time-step arguments (dgx_misc.cu)
 struct DtArgs {

@@ -31,6 +31,12 @@
 #ifndef DGX_REAL
 #error "define DGX_REAL before including dgx_stage.cuh"
 #endif
+// DGX_STAGE_BND selects the kernels this translation unit instantiates: 0 for
+// meshes without boundary sides (no ghost-state code at all), 1 for meshes with
+// them
+#ifndef DGX_STAGE_BND
+#error "define DGX_STAGE_BND (0 or 1) before including dgx_stage.cuh"
+#endif
 
 // Loops over quadrature points (and, optionally, sides) are kept rolled: the
 // fully unrolled kernel is several times larger than the instruction cache and
@@ -49,6 +55,7 @@
 namespace dgx {
 
 static __constant__ DGX_REAL c_tab[kTableTotal];
+constexpr bool kStageBnd = DGX_STAGE_BND != 0;
 
 template <typename T>
 __device__ __forceinline__ T pick3(T a0, T a1, T a2, int k) { return k == 0 ? a0 : (k == 1 ? a1 : a2); }
@@ -174,13 +181,72 @@ __device__ __forceinline__ void num_flux(const R *UL, const R *UR, R nx, R ny, i
 //   advection: the initial condition translated by a*t (the reference's
 //             boundary_exact, src/2d/2dadvec/2dadvec_kernels.cu:184-186,492-517),
 //             or the interior state when none is set.
+// Physical position of Gauss point j of local side k of element e, in FP64:
+// Vk + t_j (Vk+1 - Vk) with t_j = (1 + s_j)/2, the point the reference's
+// boundary hooks map from the element (euler.cu:186-205) written along the
+// side, so that it lies on the side for any rounding of the table (a point on
+// an axis keeps its sign)
+template <int P>
+__device__ __forceinline__ void side_point_xy(const StageArgs &a, int e, int k, int j, double &x, double &y) {
+    const size_t E = static_cast<size_t>(a.E);
+    const double *V = a.V;
+    const int kb = k == 2 ? 0 : k + 1;
+    const double t = static_cast<double>(c_tab[Lay<P>::SRS + 2 * j]);   // side 0: r = (1 + s_j)/2
+    const double xa = V[2 * k * E + e], ya = V[(2 * k + 1) * E + e];
+    x = xa + t * (V[2 * kb * E + e] - xa);
+    y = ya + t * (V[(2 * kb + 1) * E + e] - ya);
+}
+
 template <int P, int EQ>
 __device__ __noinline__ void boundary_ghost(const StageArgs &a, int tag, int k, int j, int e, const R *UO,
-                                            R nx, R ny, R xr, R yr, R xs, R ys, R *UN) {
+                                            R nx, R ny, R *UN) {
     using L = Lay<P>;
     constexpr int NQ1 = L::NQ1;
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     if constexpr (EQ == DGX_EULER) {
+        if (a.bc_kind == 3) {   // the problem file's own hooks (DGX_BC_PROBLEM)
+            const double *P = a.bc_params;
+            const double g = a.gamma;
+            double U[4];
+            if (a.bc_ic == DGX_IC_THREEPOINT && tag == -1) {
+                // flip the x momentum where m.n > 0, else the y momentum
+                // (threepoint.cu:86-109; its sqrtf(m.n) > 0 test is m.n > 0 in FP32)
+                const bool out = static_cast<float>(UO[1] * nx + UO[2] * ny) > 0.f;
+                UN[0] = UO[0];
+                UN[1] = out ? -UO[1] : UO[1];
+                UN[2] = out ? UO[2] : -UO[2];
+                UN[3] = UO[3];
+                return;
+            }
+            // side point (side 1 exchanged for the radial reflections, as the
+            // reference's reflecting_boundary maps it, cylinder.cu:78-81)
+            const int jj = (tag == -1 && k == 1) ? NQ1 - 1 - j : j;
+            double x, y;
+            side_point_xy<P>(a, e, k, jj, x, y);
+            if (tag == -1) {   // keep the momentum tangential to the circle through the point
+                const double c0 = a.bc_ic == DGX_IC_CYLINDER ? 0.5 : 0.0;
+                x -= c0;
+                y -= c0;
+                const double d = sqrt(x * x + y * y);
+                const R Nx = static_cast<R>(x / d), Ny = static_cast<R>(y / d);
+                const R tm = UO[1] * Ny - UO[2] * Nx;
+                UN[0] = UO[0];
+                UN[1] = tm * Ny;
+                UN[2] = -tm * Nx;
+                UN[3] = UO[3];
+                return;
+            }
+            if (a.bc_ic == DGX_IC_THREEPOINT) {
+                const double ang = P[1] * kRefPi / 180.0;
+                const double t = a.mode == 0 ? a.t : a.scal[2] + a.stage_c * a.scal[0];
+                if (tag == -2 || x < P[0] * t * cos(ang) + tan(ang)) threepoint_shock(P, g, U);
+                else ic_eval(DGX_IC_THREEPOINT, P, g, x, y, U);
+            } else {
+                ic_eval(a.bc_ic, P, g, x, y, U);
+            }
+            for (int n = 0; n < 4; ++n) UN[n] = static_cast<R>(U[n]);
+            return;
+        }
         if (tag == -1) {
             const R mn = UO[1] * nx + UO[2] * ny;
             UN[0] = UO[0];
@@ -194,10 +260,8 @@ __device__ __noinline__ void boundary_ghost(const StageArgs &a, int tag, int k, 
         }
     } else {
         if (a.bc_kind == 2) {
-            const double r = static_cast<double>(c_tab[L::SRS + (k * NQ1 + j) * 2]);
-            const double s = static_cast<double>(c_tab[L::SRS + (k * NQ1 + j) * 2 + 1]);
-            const double x = a.vx1[e] + static_cast<double>(xr) * r + static_cast<double>(xs) * s;
-            const double y = a.vy1[e] + static_cast<double>(yr) * r + static_cast<double>(ys) * s;
+            double x, y;
+            side_point_xy<P>(a, e, k, j, x, y);
             const double t = a.mode == 0 ? a.t : a.scal[2] + a.stage_c * a.scal[0];
             double U[4];
             ic_eval(a.bc_ic, a.bc_params, a.gamma, x - a.ax * t, y - a.ay * t, U);
@@ -235,7 +299,7 @@ DGX_HD constexpr size_t stage_smem_bytes(int nslot, int prefetch) {
 // this tile's prefetch (if any) completes; returns whether a prefetch was
 // issued (the caller then advances its phase).  All threads of the CTA call it
 // with the same arguments; on return no copy of this tile is in flight.
-template <int P, int EQ>
+template <int P, int EQ, bool BND>
 __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, unsigned char *smem_raw,
                                            const unsigned parity) {
     using L = Lay<P>;
@@ -436,7 +500,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
         const R nx = pick3(snx[0], snx[1], snx[2], k), ny = pick3(sny[0], sny[1], sny[2], k);
         const R hl = pick3(shl[0], shl[1], shl[2], k);
         const int own = 3 * tid + k;
-        const bool bnd = word < 0;              // boundary side: this element is its left element
+        const bool bnd = BND && word < 0;       // boundary side: this element is its left element
         const int slot = bnd ? own : (word >> 1);
         const int il = bnd ? 1 : (word & 1);
         const R *s_own = s_tr + own * TSW;
@@ -450,7 +514,9 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
                 UO[n] = s_own[j * NV + n];
                 UN[n] = s_nbr[(NQ1 - 1 - j) * NV + n];
             }
-            if (bnd) boundary_ghost<P, EQ>(a, word, k, j, e, UO, nx, ny, xr, yr, xs, ys, UN);
+            if constexpr (BND) {
+                if (bnd) boundary_ghost<P, EQ>(a, word, k, j, e, UO, nx, ny, UN);
+            }
 #pragma unroll
             for (int n = 0; n < NV; ++n) {
                 UL[n] = il ? UO[n] : UN[n];
@@ -571,18 +637,18 @@ template <int P>
 constexpr int min_ctas() { return P <= 3 ? DGX_MIN_CTAS_P3 : 2; }
 
 // Plain path: one CTA per tile of one solve.
-template <int P, int EQ>
+template <int P, int EQ, bool BND>
 __global__ void __launch_bounds__(kTile, min_ctas<P>()) stage_kernel(const StageArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     if (threadIdx.x == 0) mbar_init(reinterpret_cast<unsigned long long *>(smem_raw), 1);
     __syncthreads();
-    stage_tile<P, EQ>(a, blockIdx.x, smem_raw, 0u);
+    stage_tile<P, EQ, BND>(a, blockIdx.x, smem_raw, 0u);
 }
 
 // Batched path: the CTAs of one launch walk a work list of (solve, tile) items
 // of many solves of the same order and equation (grid-stride, so the launch can
 // be persistent); every solve keeps its own state, geometry and dt.
-template <int P, int EQ>
+template <int P, int EQ, bool BND>
 __global__ void __launch_bounds__(kTile, min_ctas<P>()) batch_stage_kernel(const BatchStageArgs b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     if (threadIdx.x == 0) mbar_init(reinterpret_cast<unsigned long long *>(smem_raw), 1);
@@ -598,12 +664,12 @@ __global__ void __launch_bounds__(kTile, min_ctas<P>()) batch_stage_kernel(const
             reinterpret_cast<int *>(&s_args)[threadIdx.x] =
                 reinterpret_cast<const int *>(b.args + w.x)[threadIdx.x];
         __syncthreads();
-        if (stage_tile<P, EQ>(s_args, w.y, smem_raw, phase & 1u)) ++phase;
+        if (stage_tile<P, EQ, BND>(s_args, w.y, smem_raw, phase & 1u)) ++phase;
         __syncthreads();   // shared memory is reused by the next item
     }
 }
 
-template <int P, int EQ>
+template <int P, int EQ, bool BND>
 static int launch_one(const StageArgs &a_in, cudaStream_t st) {
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     StageArgs a = a_in;
@@ -611,22 +677,22 @@ static int launch_one(const StageArgs &a_in, cudaStream_t st) {
     const size_t smem = stage_smem_bytes<P, NV>(a.nslot, a.prefetch);
     static size_t configured = 0;   // dynamic shared memory opted in so far
     if (smem > 48 * 1024 && smem > configured) {
-        DGX_TRY_CUDA(cudaFuncSetAttribute(stage_kernel<P, EQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        DGX_TRY_CUDA(cudaFuncSetAttribute(stage_kernel<P, EQ, BND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           static_cast<int>(smem)));
         // all of the unified L1 / shared storage as shared memory, so that
         // several CTAs with large tiles fit on an SM
-        DGX_TRY_CUDA(cudaFuncSetAttribute(stage_kernel<P, EQ>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        DGX_TRY_CUDA(cudaFuncSetAttribute(stage_kernel<P, EQ, BND>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                           100));
         configured = smem;
     }
     const int grid = (a.E + kTile - 1) / kTile;
-    if (grid > 0) stage_kernel<P, EQ><<<grid, kTile, smem, st>>>(a);
+    if (grid > 0) stage_kernel<P, EQ, BND><<<grid, kTile, smem, st>>>(a);
     DGX_CHECK_LAUNCH();
     return DGX_OK;
 }
 
 // Batched path, one item per CTA (the flat grid): no loop to keep live state across.
-template <int P, int EQ>
+template <int P, int EQ, bool BND>
 __global__ void __launch_bounds__(kTile, min_ctas<P>()) batch_stage_kernel_flat(const BatchStageArgs b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ StageArgs s_args;
@@ -636,25 +702,25 @@ __global__ void __launch_bounds__(kTile, min_ctas<P>()) batch_stage_kernel_flat(
     if (threadIdx.x < kWords)
         reinterpret_cast<int *>(&s_args)[threadIdx.x] = reinterpret_cast<const int *>(b.args + w.x)[threadIdx.x];
     __syncthreads();
-    stage_tile<P, EQ>(s_args, w.y, smem_raw, 0u);
+    stage_tile<P, EQ, BND>(s_args, w.y, smem_raw, 0u);
 }
 
-template <int P, int EQ>
+template <int P, int EQ, bool BND>
 static int launch_batch_one(const BatchStageArgs &b, cudaStream_t st) {
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     const size_t smem = stage_smem_bytes<P, NV>(b.nslot, b.prefetch);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
-        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel<P, EQ>,
+        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel<P, EQ, BND>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel_flat<P, EQ>,
+        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel_flat<P, EQ, BND>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel<P, EQ>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel_flat<P, EQ>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel<P, EQ, BND>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel_flat<P, EQ, BND>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         configured = smem;
     }
-    if (b.grid > 0 && b.grid >= b.n_items) batch_stage_kernel_flat<P, EQ><<<b.n_items, kTile, smem, st>>>(b);
-    else if (b.grid > 0) batch_stage_kernel<P, EQ><<<b.grid, kTile, smem, st>>>(b);
+    if (b.grid > 0 && b.grid >= b.n_items) batch_stage_kernel_flat<P, EQ, BND><<<b.n_items, kTile, smem, st>>>(b);
+    else if (b.grid > 0) batch_stage_kernel<P, EQ, BND><<<b.grid, kTile, smem, st>>>(b);
     DGX_CHECK_LAUNCH();
     return DGX_OK;
 }
@@ -676,12 +742,12 @@ static size_t batch_smem_impl(int order, int nslot, int prefetch) {
 template <int EQ>
 static int launch_batch_order(int order, const BatchStageArgs &b, cudaStream_t st) {
     switch (order) {
-    case 0: return launch_batch_one<0, EQ>(b, st);
-    case 1: return launch_batch_one<1, EQ>(b, st);
-    case 2: return launch_batch_one<2, EQ>(b, st);
-    case 3: return launch_batch_one<3, EQ>(b, st);
-    case 4: return launch_batch_one<4, EQ>(b, st);
-    case 5: return launch_batch_one<5, EQ>(b, st);
+    case 0: return launch_batch_one<0, EQ, kStageBnd>(b, st);
+    case 1: return launch_batch_one<1, EQ, kStageBnd>(b, st);
+    case 2: return launch_batch_one<2, EQ, kStageBnd>(b, st);
+    case 3: return launch_batch_one<3, EQ, kStageBnd>(b, st);
+    case 4: return launch_batch_one<4, EQ, kStageBnd>(b, st);
+    case 5: return launch_batch_one<5, EQ, kStageBnd>(b, st);
     default: set_error("unsupported order %d", order); return DGX_ERR_UNSUPPORTED;
     }
 }
@@ -689,12 +755,12 @@ static int launch_batch_order(int order, const BatchStageArgs &b, cudaStream_t s
 template <int EQ>
 static int launch_order(int order, const StageArgs &a, cudaStream_t st) {
     switch (order) {
-    case 0: return launch_one<0, EQ>(a, st);
-    case 1: return launch_one<1, EQ>(a, st);
-    case 2: return launch_one<2, EQ>(a, st);
-    case 3: return launch_one<3, EQ>(a, st);
-    case 4: return launch_one<4, EQ>(a, st);
-    case 5: return launch_one<5, EQ>(a, st);
+    case 0: return launch_one<0, EQ, kStageBnd>(a, st);
+    case 1: return launch_one<1, EQ, kStageBnd>(a, st);
+    case 2: return launch_one<2, EQ, kStageBnd>(a, st);
+    case 3: return launch_one<3, EQ, kStageBnd>(a, st);
+    case 4: return launch_one<4, EQ, kStageBnd>(a, st);
+    case 5: return launch_one<5, EQ, kStageBnd>(a, st);
     default: set_error("unsupported order %d", order); return DGX_ERR_UNSUPPORTED;
     }
 }

@@ -1,13 +1,15 @@
-// FP32 instantiation of the fused stage kernel (the plain FP32 path).
+// FP32 instantiation of the fused stage kernel (the plain FP32 path),
+// for meshes without boundary sides.
 #define DGX_REAL float
+#define DGX_STAGE_BND 0
 #include "dgx_stage.cuh"
 
 namespace dgx {
-int launch_stage_f32(int order, int equation, const StageArgs &a, cudaStream_t st) {
+int launch_stage_f32_nb(int order, int equation, const StageArgs &a, cudaStream_t st) {
     return launch_stage_impl(order, equation, a, st);
 }
-int upload_tables_f32() { return upload_tables_impl(); }
-int launch_batch_stage_f32(int order, int equation, const BatchStageArgs &b, cudaStream_t st) {
+int upload_tables_f32_nb() { return upload_tables_impl(); }
+int launch_batch_stage_f32_nb(int order, int equation, const BatchStageArgs &b, cudaStream_t st) {
     return equation == DGX_EULER ? launch_batch_order<DGX_EULER>(order, b, st)
                                  : launch_batch_order<DGX_ADVECTION>(order, b, st);
 }

@@ -23,7 +23,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 __all__ = ["Mesh", "periodic_square", "scramble", "dirichlet_square", "unit_draws", "write_pmsh",
-           "read_pmsh", "read_gmsh", "tag_boundary"]
+           "read_pmsh", "read_gmsh", "tag_boundary", "from_triangles", "annulus"]
 
 
 def _splitmix64(x: np.ndarray) -> np.ndarray:
@@ -339,32 +339,7 @@ def read_gmsh(path_or_text: str, boundary_tags=None) -> Mesh:
             tris.append((a, c, b) if J < 0 else (a, b, c))
         elif etype == 1:
             bnd[frozenset(nodes[:2])] = tags.get(phys, -1)
-    E = len(tris)
-    es = np.zeros((E, 3), dtype=np.int64)
-    le, re, ls, rs = [], [], [], []
-    side_of = {}
-    for e, t in enumerate(tris):
-        for k in range(3):
-            key = frozenset((t[k], t[(k + 1) % 3]))
-            if key in side_of:
-                s = side_of[key]
-                re[s], rs[s] = e, k
-            else:
-                s = len(le)
-                side_of[key] = s
-                le.append(e); ls.append(k); re.append(bnd.get(key, -1)); rs.append(-1)
-            es[e, k] = s
-    le, re, ls, rs = (np.array(x, dtype=np.int64) for x in (le, re, ls, rs))
-    order = np.concatenate([np.nonzero(re == t)[0] for t in (-1, -2, -3)] + [np.nonzero(re >= 0)[0]])
-    inv = np.empty_like(order)
-    inv[order] = np.arange(order.size)
-    es = inv[es]
-    T = np.array(tris)
-    V = [xy[T[:, 0], 0], xy[T[:, 0], 1], xy[T[:, 1], 0], xy[T[:, 1], 1], xy[T[:, 2], 0], xy[T[:, 2], 1]]
-    m = Mesh(*V, es[:, 0], es[:, 1], es[:, 2], le[order], re[order], ls[order], rs[order],
-             meta=dict(kind="gmsh"))
-    m.check()
-    return m
+    return from_triangles(xy, tris, lambda a, b: bnd.get(frozenset((a, b)), -1), kind="gmsh")
 
 
 def tag_boundary(mesh: Mesh, fn) -> Mesh:
@@ -378,3 +353,101 @@ def tag_boundary(mesh: Mesh, fn) -> Mesh:
         re[s] = int(fn(0.5 * (a[0] + b[0]), 0.5 * (a[1] + b[1])))
     return Mesh(*mesh.vertices(), *mesh.elem_sides(), mesh.left_elem, re, mesh.left_side,
                 mesh.right_side, meta=dict(mesh.meta, tagged=True))
+
+
+def from_triangles(xy, tris, boundary_tag, kind: str = "triangles") -> Mesh:
+    """Vertices ``xy[n, 2]`` and counter-clockwise triangles ``tris[E, 3]`` (vertex
+    indices) -> Mesh.  Sides are matched by their vertex pair, the first
+    element to meet a side is its left element; an unmatched side is a
+    boundary side tagged ``boundary_tag(a, b)`` (its vertex indices, in the left
+    element's order).  Boundary sides come first, in the order -1, -2, -3, as
+    the reference's converter sorts them (genmesh.py:244-284)."""
+    xy = np.asarray(xy, dtype=np.float64)
+    T = np.asarray(tris, dtype=np.int64)
+    E = T.shape[0]
+    es = np.zeros((E, 3), dtype=np.int64)
+    le, re, ls, rs, ends = [], [], [], [], []
+    side_of = {}
+    for e in range(E):
+        t = T[e]
+        for k in range(3):
+            a, b = int(t[k]), int(t[(k + 1) % 3])
+            key = (a, b) if a < b else (b, a)
+            if key in side_of:
+                q = side_of.pop(key)
+                re[q], rs[q] = e, k
+            else:
+                q = len(le)
+                side_of[key] = q
+                le.append(e); ls.append(k); re.append(-1); rs.append(-1); ends.append((a, b))
+            es[e, k] = q
+    for q in side_of.values():   # sides met once: boundary sides
+        re[q] = int(boundary_tag(*ends[q]))
+    le, re, ls, rs = (np.array(x, dtype=np.int64) for x in (le, re, ls, rs))
+    order = np.concatenate([np.nonzero(re == t)[0] for t in (-1, -2, -3)] + [np.nonzero(re >= 0)[0]])
+    if order.size != le.size:
+        raise ValueError("boundary tags must be -1, -2 or -3")
+    inv = np.empty_like(order)
+    inv[order] = np.arange(order.size)
+    es = inv[es]
+    V = [xy[T[:, 0], 0], xy[T[:, 0], 1], xy[T[:, 1], 0], xy[T[:, 1], 1], xy[T[:, 2], 0], xy[T[:, 2], 1]]
+    m = Mesh(*V, es[:, 0], es[:, 1], es[:, 2], le[order], re[order], ls[order], rs[order],
+             meta=dict(kind=kind))
+    m.check()
+    return m
+
+
+def annulus(nr: int, nt: int, r0: float, r1: float, theta0: float = 0.0,
+            theta1: float = 2.0 * np.pi, cx: float = 0.0, cy: float = 0.0,
+            tag=None) -> Mesh:
+    """Structured triangulation of the ring sector r0 <= r <= r1,
+    theta0 <= theta <= theta1 about (cx, cy): nr x nt cells, each split into
+    two counter-clockwise triangles.  A full ring (theta1 - theta0 = 2 pi)
+    closes on itself.  ``tag(x_mid, y_mid, where)`` gives each boundary side's
+    tag, ``where`` one of "inner", "outer", "start", "end"; the default tags
+    the arcs -1 (reflecting walls), the start ray -3 (inflow) and the end ray -2
+    (outflow).  The meshes of the reference's cylinder and supersonic-vortex
+    problems are of this kind."""
+    full = abs((theta1 - theta0) - 2.0 * np.pi) < 1e-12
+    ntv = nt if full else nt + 1
+    r = np.linspace(r0, r1, nr + 1)
+    th = theta0 + (theta1 - theta0) * np.arange(ntv) / nt
+    R, TH = np.meshgrid(r, th, indexing="ij")
+    xy = np.stack([cx + R * np.cos(TH), cy + R * np.sin(TH)], axis=-1).reshape(-1, 2)
+
+    def vid(i, j):
+        return i * ntv + (j % ntv if full else j)
+
+    tris = []
+    for i in range(nr):
+        for j in range(nt):
+            a, b, c, d = vid(i, j), vid(i + 1, j), vid(i + 1, j + 1), vid(i, j + 1)
+            tris.append((a, b, c))
+            tris.append((a, c, d))
+    tris = np.array(tris)
+    J = ((xy[tris[:, 1], 0] - xy[tris[:, 0], 0]) * (xy[tris[:, 2], 1] - xy[tris[:, 0], 1])
+         - (xy[tris[:, 2], 0] - xy[tris[:, 0], 0]) * (xy[tris[:, 1], 1] - xy[tris[:, 0], 1]))
+    flip = J < 0
+    tris[flip] = tris[flip][:, [0, 2, 1]]
+
+    def where(a, b):
+        ia, ja = divmod(a, ntv)
+        ib, jb = divmod(b, ntv)
+        if ia == ib == 0:
+            return "inner"
+        if ia == ib == nr:
+            return "outer"
+        return "start" if ja == jb == 0 else "end"
+
+    default = {"inner": -1, "outer": -1, "start": -3, "end": -2}
+
+    def btag(a, b):
+        w = where(a, b)
+        if tag is None:
+            return default[w]
+        xm, ym = 0.5 * (xy[a] + xy[b])
+        return tag(xm, ym, w)
+
+    m = from_triangles(xy, tris, btag, kind="annulus")
+    m.meta.update(nr=nr, nt=nt, r0=r0, r1=r1, theta0=theta0, theta1=theta1, cx=cx, cy=cy)
+    return m

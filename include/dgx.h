@@ -269,10 +269,22 @@ int dgx_solver_set_option(dgx_solver *solver, int option, int value);
 /* Number of CUDA kernels this solver has launched so far. */
 int dgx_launch_count(const dgx_solver *solver, long long *count);
 
+/* Tensor-core self-test on the current device.  No reference counterpart.
+ * One CTA multiplies a 128x16 by 16x32 matrix of small integers in BF16 with
+ * tcgen05.mma (FP32 accumulation), A once from shared and once from tensor
+ * memory, and counts the accumulator elements that differ from the exact
+ * product: *bad_ss (A in shared memory) and *bad_ts (A in tensor memory); both
+ * 0 means the path works.  variant 0 is the operand-descriptor encoding the
+ * solvers use, variant 1 the same layout with the two descriptor offsets
+ * exchanged (a diagnostic).  `values` (optional, 128 x 64 floats) receives the
+ * two accumulators row by row.  DGX_ERR_TIMEOUT if the MMA did not complete. */
+int dgx_tc_selftest(int variant, int *bad_ss, int *bad_ts, float *values);
+
 /* --- batches: many independent solves per launch --------------------------- */
 /* New, no counterpart in the reference (it runs one solve per process; this
  * generalises its loop, src/2d/conservation/time_integrator.cu:252-429).
- * Solves of equal (precision, order, equation) form a class; each RK stage
+ * Solves of equal (precision, order, equation, boundary sides or none) form a
+ * class; each RK stage
  * launches one kernel per class over work lists of (solve, element tile), one
  * batched kernel computes every solve's dt, and the whole step is captured as
  * a CUDA graph.  Every solve keeps its own state, time, dt rule and end time

@@ -503,16 +503,16 @@ static void orc_phys_flux(const orc_solver *S, const double *U, double *fx, doub
  * euler.cu:177-241) or the interior state; advection takes the initial
  * condition translated by a*t (boundary_exact, 2dadvec_kernels.cu:184-186) or
  * the interior state. */
-/* point j of local side ls of element L (the mapping of inflow_boundary,
- * euler.cu:186-205) */
+/* point j of local side ls of element L: the point the reference's hooks map
+ * from the element, x = V2 r + V3 s + V1 (1 - r - s) (inflow_boundary,
+ * euler.cu:186-205), written along the side as Va + t (Vb - Va) with
+ * t = (1 + s_j)/2 so that it lies on the side for any rounding */
 static void orc_side_xy(const orc_solver *S, int L, int ls, int j, double *x, double *y) {
-    const orc_tables *T = &S->T;
-    double g = T->s1[j], gr = T->s1[T->nq1 - 1 - j], r, s;
-    if (ls == 0) { r = 0.5 + 0.5 * g; s = 0.0; }
-    else if (ls == 1) { r = (1.0 - g) / 2.0; s = (1.0 + g) / 2.0; }
-    else { r = 0.0; s = 0.5 + 0.5 * gr; }
-    *x = S->V[0][L] + S->xr[L] * r + S->xs[L] * s;
-    *y = S->V[1][L] + S->yr[L] * r + S->ys[L] * s;
+    int kb = ls == 2 ? 0 : ls + 1;
+    double t = 0.5 + 0.5 * S->T.s1[j];
+    double xa = S->V[2 * ls][L], ya = S->V[2 * ls + 1][L];
+    *x = xa + t * (S->V[2 * kb][L] - xa);
+    *y = ya + t * (S->V[2 * kb + 1][L] - ya);
 }
 
 /* Problem ghost states (DGX_BC_PROBLEM), the reference's problem hooks:
