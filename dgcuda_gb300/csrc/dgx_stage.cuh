@@ -169,18 +169,6 @@ __device__ __forceinline__ void num_flux(const R *UL, const R *UR, R nx, R ny, i
     }
 }
 
-// Ghost state on a boundary side (the element is the side's left element, n
-// points out of the domain), at the side's point j in this element's order:
-//   Euler  -1 reflecting: density and energy kept, momentum reduced to its
-//             tangential part (the reference's reflecting_boundary,
-//             src/2d/conservation/euler/cylinder/cylinder.cu:58-111, with the
-//             side's normal);
-//          -2 outflow, -3 inflow: the solver's free-stream state (the problem
-//             hooks U_outflow / U_inflow, src/2d/conservation/euler/euler.cu:177-241),
-//             or the interior state when none is set;
-//   advection: the initial condition translated by a*t (the reference's
-//             boundary_exact, src/2d/2dadvec/2dadvec_kernels.cu:184-186,492-517),
-//             or the interior state when none is set.
 // Physical position of Gauss point j of local side k of element e, in FP64:
 // Vk + t_j (Vk+1 - Vk) with t_j = (1 + s_j)/2, the point the reference's
 // boundary hooks map from the element (euler.cu:186-205) written along the
@@ -197,6 +185,18 @@ __device__ __forceinline__ void side_point_xy(const StageArgs &a, int e, int k, 
     y = ya + t * (V[(2 * kb + 1) * E + e] - ya);
 }
 
+// Ghost state on a boundary side (the element is the side's left element, n
+// points out of the domain), at the side's point j in this element's order:
+//   Euler  -1 reflecting: density and energy kept, momentum reduced to its
+//             tangential part (the reference's reflecting_boundary,
+//             src/2d/conservation/euler/cylinder/cylinder.cu:58-111, with the
+//             side's normal);
+//          -2 outflow, -3 inflow: the solver's free-stream state (the problem
+//             hooks U_outflow / U_inflow, src/2d/conservation/euler/euler.cu:177-241),
+//             or the interior state when none is set;
+//   advection: the initial condition translated by a*t (the reference's
+//             boundary_exact, src/2d/2dadvec/2dadvec_kernels.cu:184-186,492-517),
+//             or the interior state when none is set.
 template <int P, int EQ>
 __device__ __noinline__ void boundary_ghost(const StageArgs &a, int tag, int k, int j, int e, const R *UO,
                                             R nx, R ny, R *UN) {
@@ -205,7 +205,7 @@ __device__ __noinline__ void boundary_ghost(const StageArgs &a, int tag, int k, 
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     if constexpr (EQ == DGX_EULER) {
         if (a.bc_kind == 3) {   // the problem file's own hooks (DGX_BC_PROBLEM)
-            const double *P = a.bc_params;
+            const double *prm = a.bc_params;
             const double g = a.gamma;
             double U[4];
             if (a.bc_ic == DGX_IC_THREEPOINT && tag == -1) {
@@ -237,12 +237,12 @@ __device__ __noinline__ void boundary_ghost(const StageArgs &a, int tag, int k, 
                 return;
             }
             if (a.bc_ic == DGX_IC_THREEPOINT) {
-                const double ang = P[1] * kRefPi / 180.0;
+                const double ang = prm[1] * kRefPi / 180.0;
                 const double t = a.mode == 0 ? a.t : a.scal[2] + a.stage_c * a.scal[0];
-                if (tag == -2 || x < P[0] * t * cos(ang) + tan(ang)) threepoint_shock(P, g, U);
-                else ic_eval(DGX_IC_THREEPOINT, P, g, x, y, U);
+                if (tag == -2 || x < prm[0] * t * cos(ang) + tan(ang)) threepoint_shock(prm, g, U);
+                else ic_eval(DGX_IC_THREEPOINT, prm, g, x, y, U);
             } else {
-                ic_eval(a.bc_ic, P, g, x, y, U);
+                ic_eval(a.bc_ic, prm, g, x, y, U);
             }
             for (int n = 0; n < 4; ++n) UN[n] = static_cast<R>(U[n]);
             return;
