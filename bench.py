@@ -35,11 +35,15 @@ sys.path.insert(0, ROOT)
 
 METRIC = "DOF-updates/s on 1 GB300, served/batched vs plain at L2≤1e-5; p50/p99 latency"
 UNIT = "DOF-updates/s"
-WORKLOAD = dict(workload="euler_density_wave_2x1024^2_p3", equation="euler", order=3,
-                num_elem=2 * 1024 * 1024, mesh="periodic 2x1024^2, jitter 0.15h, seed 12347",
+def workload(n: int) -> dict:
+    """Labels of the density-wave workload on the 2 x n^2 mesh."""
+    mb = 2 * n * n * 40 * 4 / 1e6
+    return dict(workload=f"euler_density_wave_2x{n}^2_p3", equation="euler", order=3,
+                num_elem=2 * n * n, mesh=f"periodic 2x{n}^2, jitter 0.15h, seed 12347",
                 ic="rho=1+0.2 sin(2pi(x+y)), u=v=1, p=1, gamma=1.4", flux="LLF",
                 integrator="RK4, CFL 0.7 on device", precision="fp32",
-                l2_flush="inputs larger than L2 (4 state vectors x 335.5 MB)")
+                l2_flush=f"inputs larger than L2 (4 state vectors x {mb:.1f} MB)" if 4 * mb > 129
+                else f"inputs of 4 x {mb:.1f} MB (not larger than L2)")
 
 
 def peaks():
@@ -168,7 +172,7 @@ def run_reference(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": WORKLOAD, "impl": "reference",
+        "config": workload(args.mesh_n), "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -228,7 +232,7 @@ def _native_solver(spec):
     return sv
 
 
-def run_accuracy(mesh_n: int, steps: int = 100):
+def run_accuracy(mesh_n: int, steps: int = 100, precision=None):
     """Config-3 accuracy: the FP32 path and the FP64 path on the same mesh and
     initial state for `steps` RK4 steps with the same fixed dt (the FP32 run's
     first CFL dt); relative L2 per conserved variable of FP32 against FP64, and
@@ -237,13 +241,15 @@ def run_accuracy(mesh_n: int, steps: int = 100):
     holds it to 1e-11 of the CPU oracle on smaller meshes."""
     from dgcuda_gb300 import _ffi
     from dgcuda_gb300.solver import DeviceMesh, Solver
+    if precision is None:
+        precision = _ffi.FP32
     dm = DeviceMesh.periodic_square(mesh_n, 1.0, 1.0, 0.15, 12347)
     res = {}
-    for prec in (_ffi.FP32, _ffi.FP64):
+    for prec in (precision, _ffi.FP64):
         sv = Solver(dm, 3, _ffi.EULER, _ffi.FLUX_LLF, prec, 1.4)
         sv.project(_ffi.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
         res[prec] = sv
-    s32, s64 = res[_ffi.FP32], res[_ffi.FP64]
+    s32, s64 = res[precision], res[_ffi.FP64]
     s32.set_dt(None)
     s32.run(max_steps=1)
     _, dt = s32.time()
@@ -365,41 +371,22 @@ def run_served(rates=(50, 200, 1000, 2000), count: int = 400):
             "rates": out, "plain_value": plain, "unit": UNIT}
 
 
-def run_ours(args, rank, world, local):
+def time_steps(sv, steps, warmup, stream, world):
+    """W untimed steps, then K steps timed with CUDA events on `stream`;
+    returns (ms per step, mean ms of stages 2-4, kernel launches, wall start, wall end)."""
     import torch
-    torch.cuda.set_device(local)
-    from dgcuda_gb300 import _ffi, build
-    from dgcuda_gb300.solver import Solver
-    build.build()
-    n = args.mesh_n
-    mesh = build_mesh(n)
-    E = mesh.num_elem
-    sv = Solver(mesh, 3, _ffi.EULER, _ffi.FLUX_LLF, _ffi.FP32, 1.4)
-    sv.project(_ffi.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
-    sv.set_dt(None, cfl=0.7)
-    sv.set_end_time(0.0)
-    stream = torch.cuda.Stream()
     sh = stream.cuda_stream
-    dofs = 4 * 10 * E
-    X = dofs * 4
-    G = 20 * E + 24 * mesh.num_sides
-    step_bytes = 16 * X + 4 * G                   # algorithmic bytes per RK4 step
-    # stages 2, 3, 4 move 5X + G, 5X + G and 3X + G (stage 1: 3X + G, timed with the CFL kernel)
-    stage_bytes = (13 * X + 3 * G) / 3.0          # per timed stage launch (average)
-
-    clocks = ClockSampler(local)
-    clocks.start()
     with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             sv.step(sh)
         torch.cuda.synchronize()
         launches0 = sv.launch_count()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-               torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+               torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         barrier(world)
         torch.cuda.synchronize()
         t_wall0 = time.time()
-        for i in range(args.steps):
+        for i in range(steps):
             ev[i][0].record(stream)
             sv.rk_stage(0, sh)        # CFL reduction + dt, then stage 1
             ev[i][1].record(stream)
@@ -412,8 +399,64 @@ def run_ours(args, rank, world, local):
         t_wall1 = time.time()
         launches = sv.launch_count() - launches0
     total_ms = ev[0][0].elapsed_time(ev[-1][2])
-    ms_step = allreduce_max(total_ms / args.steps, world)
-    stage_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / (3 * args.steps)   # stages 2-4
+    ms_step = allreduce_max(total_ms / steps, world)
+    stage_ms = sum(e[1].elapsed_time(e[2]) for e in ev) / (3 * steps)   # stages 2-4
+    return ms_step, stage_ms, launches, t_wall0, t_wall1
+
+
+def density_wave_solver(mesh, precision):
+    from dgcuda_gb300 import _ffi
+    from dgcuda_gb300.solver import Solver
+    sv = Solver(mesh, 3, _ffi.EULER, _ffi.FLUX_LLF, precision, 1.4)
+    sv.project(_ffi.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
+    sv.set_dt(None, cfl=0.7)
+    sv.set_end_time(0.0)
+    return sv
+
+
+def run_bf16x3(mesh, args, stage_bytes, peak, dofs, fp32_ms):
+    """The same workload with the basis contractions on the tensor cores
+    (DGX_FP32_BF16X3): step time, roofline fraction of its stage kernel, and
+    accuracy against the FP64 path after 100 steps from the same state."""
+    import torch
+    from dgcuda_gb300 import _ffi
+    try:
+        sv = density_wave_solver(mesh, _ffi.FP32_BF16X3)
+    except Exception as exc:   # e.g. the tensor-core self-test refused the device
+        return {"unavailable": str(exc)}
+    stream = torch.cuda.Stream()
+    ms, stage_ms, launches, _, _ = time_steps(sv, args.steps, args.warmup, stream, 1)
+    achieved = stage_bytes / (stage_ms * 1e-3) / 1e9
+    acc = run_accuracy(args.mesh_n, precision=_ffi.FP32_BF16X3)
+    return {"value": dofs / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "speedup_vs_fp32": fp32_ms / ms,
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "kernel": "stage_kernel_tc<3,EULER> (fused RK4 stage, BF16x3 MMA)"},
+            "accuracy": acc}
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    torch.cuda.set_device(local)
+    from dgcuda_gb300 import _ffi, build
+    build.build()
+    n = args.mesh_n
+    mesh = build_mesh(n)
+    E = mesh.num_elem
+    prec = _ffi.FP32_BF16X3 if args.precision == "bf16x3" else _ffi.FP32
+    sv = density_wave_solver(mesh, prec)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    dofs = 4 * 10 * E
+    X = dofs * 4
+    G = 20 * E + 24 * mesh.num_sides
+    step_bytes = 16 * X + 4 * G                   # algorithmic bytes per RK4 step
+    # stages 2, 3, 4 move 5X + G, 5X + G and 3X + G (stage 1: 3X + G, timed with the CFL kernel)
+    stage_bytes = (13 * X + 3 * G) / 3.0          # per timed stage launch (average)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms_step, stage_ms, launches, t_wall0, t_wall1 = time_steps(sv, args.steps, args.warmup, stream, world)
     value = dofs * world / (ms_step * 1e-3)
 
     # end to end through the C ABI with host buffers: pinned state in, step, state out
@@ -444,8 +487,9 @@ def run_ours(args, rank, world, local):
     peak, peak_src = peaks()
     achieved = stage_bytes / (stage_ms * 1e-3) / 1e9
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "stage_kernel_density_wave_p3.json")
-    if os.path.exists(prof):
+    prof = os.path.join(ROOT, "profiles", "stage_kernel_density_wave_p3.json" if prec == _ffi.FP32
+                        else "stage_kernel_tc_density_wave_p3.json")
+    if os.path.exists(prof) and n == 1024:
         try:
             traffic = json.load(open(prof)).get("dram_bytes_per_launch")
         except Exception:
@@ -454,11 +498,12 @@ def run_ours(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(WORKLOAD, num_elem=E, num_sides=mesh.num_sides, dofs=dofs,
+        "config": dict(workload(n), precision=args.precision, num_elem=E, num_sides=mesh.num_sides, dofs=dofs,
                        parallelism="replicas" if world > 1 else "single"),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "stage_kernel<3,EULER> (fused RK4 stage, FP32)",
+                     "kernel": ("stage_kernel_tc<3,EULER> (fused RK4 stage, BF16x3 MMA)" if prec != _ffi.FP32
+                                else "stage_kernel<3,EULER> (fused RK4 stage, FP32)"),
                      "algorithmic_bytes_per_launch": stage_bytes,
                      "peak_source": f"{peak_src} hbm_gbs"},
         "e2e": {"value": dofs * world / (e2e_ms * 1e-3), "unit": UNIT,
@@ -469,7 +514,8 @@ def run_ours(args, rank, world, local):
     }
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_sample()
-    if not args.no_extra:
+    if not args.no_extra and prec == _ffi.FP32:
+        out["bf16x3"] = run_bf16x3(mesh, args, stage_bytes, peak, dofs, ms_step)
         out["accuracy"] = run_accuracy(args.mesh_n)
         out["batched"] = run_batched()
         out["served"] = run_served()
@@ -483,6 +529,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mesh-n", type=int, default=1024)
+    ap.add_argument("--precision", choices=["fp32", "bf16x3"], default="fp32",
+                    help="arithmetic of the timed path: plain FP32, or FP32 with the basis "
+                         "contractions on the tensor cores (BF16x3)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and served sections")
     args = ap.parse_args()

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "dgx_internal.h"
+#include "dgx_tc_layout.h"
 
 namespace dgx {
 
@@ -18,6 +19,39 @@ namespace {
 thread_local char g_err[512] = "";
 std::mutex g_init_mu;
 bool g_tables_ready[64] = {false};
+
+// The BF16x3 path: its tables, and the tensor-core self-test passed once on
+// this device (dgx_tc_selftest).
+bool g_tc_ready[64] = {};
+int ensure_tensor_cores() {
+    int dev = 0;
+    DGX_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) { set_error("device index %d out of range", dev); return DGX_ERR_UNSUPPORTED; }
+    {
+        std::lock_guard<std::mutex> lk(g_init_mu);
+        if (g_tc_ready[dev]) return DGX_OK;
+    }
+    int major = 0, minor = 0;
+    DGX_TRY_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    DGX_TRY_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+    if (major != 10 || minor != 3) {
+        set_error("the BF16x3 path is built for sm_103a; this device is sm_%d%d", major, minor);
+        return DGX_ERR_UNSUPPORTED;
+    }
+    int bad_ss = -1, bad_ts = -1;
+    int rc = dgx_tc_selftest(0, &bad_ss, &bad_ts, nullptr);
+    if (rc) return rc;
+    if (bad_ss || bad_ts) {
+        set_error("tensor-core self-test failed (%d, %d wrong elements)", bad_ss, bad_ts);
+        return DGX_ERR_UNSUPPORTED;
+    }
+    rc = tc_images_upload();
+    if (!rc) rc = upload_tables_tc();
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    g_tc_ready[dev] = true;
+    return DGX_OK;
+}
 
 int ensure_device_tables() {
     int dev = 0;
@@ -194,6 +228,7 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
     for (int i = 0; i < 8; ++i) a.bc_params[i] = s.bc_params[i];
     a.V = m.V;
     a.bnd = m.num_boundary > 0 ? 1 : 0;
+    a.tc_img = s.precision == DGX_FP32_BF16X3 ? tc_image(s.order) : nullptr;
     if (s.precision == DGX_FP64) {
         a.geo = m.geo64;
         a.fn = m.fn64;
@@ -380,9 +415,17 @@ int dgx_solver_create(dgx_mesh *mesh, const dgx_solver_desc *desc, dgx_solver **
     if (desc->order < 0 || desc->order > kMaxOrder) { set_error("order %d outside 0..%d", desc->order, kMaxOrder); return DGX_ERR_UNSUPPORTED; }
     if (desc->equation != DGX_ADVECTION && desc->equation != DGX_EULER) { set_error("unknown equation"); return DGX_ERR_INVALID; }
     if (desc->flux != DGX_FLUX_CENTRAL && desc->flux != DGX_FLUX_LLF) { set_error("unknown flux"); return DGX_ERR_INVALID; }
-    if (desc->precision != DGX_FP32 && desc->precision != DGX_FP64) {
-        set_error("precision %d is not served by this build", desc->precision);
-        return DGX_ERR_UNSUPPORTED;
+    if (desc->precision != DGX_FP32 && desc->precision != DGX_FP64 && desc->precision != DGX_FP32_BF16X3) {
+        set_error("unknown precision %d", desc->precision);
+        return DGX_ERR_INVALID;
+    }
+    if (desc->precision == DGX_FP32_BF16X3) {
+        if (desc->order < kTcMinOrder || desc->order > kTcMaxOrder) {
+            set_error("the BF16x3 path serves orders %d..%d", kTcMinOrder, kTcMaxOrder);
+            return DGX_ERR_UNSUPPORTED;
+        }
+        int rc = ensure_tensor_cores();
+        if (rc) return rc;
     }
     if (desc->integrator != DGX_RK4 && desc->integrator != DGX_RK2 && desc->integrator != DGX_FE) {
         set_error("unknown integrator %d", desc->integrator);

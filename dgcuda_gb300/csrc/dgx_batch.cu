@@ -220,6 +220,11 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
         if (!solvers[i]) { set_error("solver %d is NULL", i); batch_free(b); return DGX_ERR_INVALID; }
         for (int j = 0; j < i; ++j)
             if (solvers[j] == solvers[i]) { set_error("solver %d appears twice", i); batch_free(b); return DGX_ERR_INVALID; }
+        if (solvers[i]->s.precision == DGX_FP32_BF16X3) {
+            set_error("solver %d: batches take FP32 and FP64 solvers", i);
+            batch_free(b);
+            return DGX_ERR_UNSUPPORTED;
+        }
         if (solvers[i]->s.integrator != DGX_RK4) {
             set_error("solver %d: batches take RK4 solvers only", i);
             batch_free(b);

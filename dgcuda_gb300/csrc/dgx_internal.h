@@ -160,6 +160,7 @@ struct StageArgs {
     double bc_params[8];
     const double *V;           // element vertices V1x, V1y, V2x, V2y, V3x, V3y [6][E] (FP64)
     int bnd;                   // the mesh has boundary sides (selects the kernels with ghost states)
+    const void *tc_img;        // BF16x3 path: the order's constant tensor-core operands (device)
 };
 
 // Batched launch: items[i] = (index into args, tile); grid CTAs walk the list.
@@ -184,7 +185,13 @@ int launch_batch_stage_f64_nb(int order, int equation, const BatchStageArgs &b, 
 int launch_batch_stage_f64_b(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
 size_t batch_smem_f32(int order, int equation, int nslot, int prefetch);
 size_t batch_smem_f64(int order, int equation, int nslot, int prefetch);
+// the BF16x3 tensor-core kernels (dgx_stage_tc.cu) and their tables
+int launch_stage_tc(int order, int equation, const StageArgs &a, cudaStream_t st);
+int upload_tables_tc();
+int tc_images_upload();          // the constant B operands, once per device (dgx_tc_tables.cpp)
+const void *tc_image(int order); // their device copy for an order (1..4) on the current device
 inline int launch_stage(int precision, int order, int equation, const StageArgs &a, cudaStream_t st) {
+    if (precision == DGX_FP32_BF16X3) return launch_stage_tc(order, equation, a, st);
     if (precision == DGX_FP64)
         return a.bnd ? launch_stage_f64_b(order, equation, a, st) : launch_stage_f64_nb(order, equation, a, st);
     return a.bnd ? launch_stage_f32_b(order, equation, a, st) : launch_stage_f32_nb(order, equation, a, st);

@@ -299,6 +299,145 @@ DGX_HD constexpr size_t stage_smem_bytes(int nslot, int prefetch) {
 // this tile's prefetch (if any) completes; returns whether a prefetch was
 // issued (the caller then advances its phase).  All threads of the CTA call it
 // with the same arguments; on return no copy of this tile is in flight.
+// Start the TMA bulk copies of the tile's epilogue operands (modes 2..4: the
+// base state for 2, 3 and the accumulator for 2, 3, 4) into `s_pre`, completing
+// on `bar`; returns whether copies were issued.
+template <int P, int NV>
+__device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, unsigned long long *bar, R *s_pre,
+                                               int tid) {
+    constexpr int NP = num_modes(P);
+    const int E = a.E;
+    const size_t SE = static_cast<size_t>(E);
+    const bool pre = a.prefetch && a.mode >= 2 && a.mode <= 4;
+    if (pre && tid < 32) {
+        // order this CTA's earlier generic-proxy accesses of the shared memory
+        // (a previous tile) before the bulk copies that overwrite it
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const int cnt = min(kTile, E - tile * kTile);
+        const unsigned bytes = static_cast<unsigned>(cnt * sizeof(R));
+        const int nplanes = NV * NP;
+        const int ncopy = (a.mode == 4) ? nplanes : 2 * nplanes;
+        if (tid == 0) mbar_expect_tx(bar, bytes * ncopy);
+        __syncwarp();
+        for (int q = tid; q < ncopy; q += 32) {
+            // planes [0, nplanes): base state (modes 2, 3), then the accumulator;
+            // mode 4 copies only the accumulator, to planes [0, nplanes)
+            const int which = (a.mode == 4) ? 1 : (q >= nplanes);
+            const int pl = q % nplanes;
+            const R *src = static_cast<const R *>(which ? a.acc : a.c) + pl * SE + static_cast<size_t>(tile) * kTile;
+            bulk_copy_g2s(s_pre + static_cast<size_t>(q) * kTile, src, bytes, bar);
+        }
+    }
+
+    return pre;
+}
+
+// Mass inverse and the RK combination of the stage (time_integrator.cu:194-218,
+// 445-464, 622-700): k = dt/J rhs, then per mode of the kernel
+//   0 k;  1 u2 = c + k/2, acc = c + k/6;  2/3 u = c + alpha k, acc += k/3;
+//   4 c = acc + k/6;  5 out = u + alpha k;  6 out = c + alpha k.
+// Waits (bounded) for the tile's prefetched base state and accumulator when
+// `pre`; returns `pre`.
+template <int P, int EQ>
+__device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs)[(EQ == DGX_EULER) ? 4 : 1][num_modes(P)],
+                                               const R (&c)[(EQ == DGX_EULER) ? 4 : 1][num_modes(P)], R dt, R invJ,
+                                               int e, size_t SE, bool pre, const R *s_pre,
+                                               unsigned long long *bar, unsigned parity, int tid) {
+    constexpr int NP = num_modes(P);
+    constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
+    const R sc = dt * invJ;
+    R *__restrict__ out = static_cast<R *>(a.out);
+    const R *pc = nullptr, *pacc = nullptr;   // base state / accumulator of this element
+    size_t pstride = SE;
+    if (pre) {
+        if (!mbar_wait_bounded(bar, parity, 1ll << 26)) {
+            // the copies did not land in time: report, wait once more for the
+            // copies still in flight (they write this CTA's shared memory), skip
+            atomicOr(a.status, kStatusCopyTimeout);
+            mbar_wait_bounded(bar, parity, 1ll << 28);
+            return pre;
+        }
+        pc = s_pre + tid;
+        pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * kTile) + tid;
+        pstride = kTile;
+    } else {
+        pc = static_cast<const R *>(a.c) + e;
+        pacc = static_cast<const R *>(a.acc) + e;
+    }
+    switch (a.mode) {
+    case 0:
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) out[(n * NP + i) * SE + e] = sc * rhs[n][i];
+        break;
+    case 1: {   // u2 = c + k1/2, acc = c + k1/6
+        R *__restrict__ acc = static_cast<R *>(a.acc);
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const R kk = sc * rhs[n][i];
+                const size_t o = (n * NP + i) * SE + e;
+                out[o] = fma(R(0.5), kk, c[n][i]);
+                acc[o] = fma(R(1.0 / 6.0), kk, c[n][i]);
+            }
+        break;
+    }
+    case 2:     // u3 = c + k2/2, acc += k2/3
+    case 3: {   // u4 = c + k3,   acc += k3/3
+        R *__restrict__ acc = static_cast<R *>(a.acc);
+        const R alpha = a.mode == 2 ? R(0.5) : R(1);
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const R kk = sc * rhs[n][i];
+                const size_t o = (n * NP + i) * SE + e;
+                const size_t po = (n * NP + i) * pstride;
+                out[o] = fma(alpha, kk, pc[po]);
+                acc[o] = fma(R(1.0 / 3.0), kk, pacc[po]);
+            }
+        break;
+    }
+    case 4: {   // c = acc + k4/6
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const size_t o = (n * NP + i) * SE + e;
+                out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], pacc[(n * NP + i) * pstride]);
+            }
+        break;
+    }
+    case 5: {   // out = u + alpha k (RK2 first stage, forward Euler)
+        const R alpha = R(a.alpha);
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) out[(n * NP + i) * SE + e] = fma(alpha, sc * rhs[n][i], c[n][i]);
+        break;
+    }
+    default: {  // 6: out = c + alpha k (RK2 second stage).  out may be the base
+                // state itself: each thread reads and then writes only its own
+                // element's values, and no other thread reads them
+        const R alpha = R(a.alpha);
+        const R *pb = static_cast<const R *>(a.c) + e;
+        R *po = static_cast<R *>(a.out) + e;
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                const size_t o = (n * NP + i) * SE;
+                const R base = pb[o];
+                po[o] = fma(alpha, sc * rhs[n][i], base);
+            }
+        break;
+    }
+    }
+    return pre;
+}
+
 template <int P, int EQ, bool BND>
 __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, unsigned char *smem_raw,
                                            const unsigned parity) {
@@ -338,26 +477,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
 
     // modes 2..4 read the base state (2, 3) and the accumulator (2, 3, 4) at the
     // end: start their copies now
-    const bool pre = a.prefetch && a.mode >= 2 && a.mode <= 4;
-    if (pre && tid < 32) {
-        // order this CTA's earlier generic-proxy accesses of the shared memory
-        // (a previous tile) before the bulk copies that overwrite it
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        const int cnt = min(kTile, E - tile * kTile);
-        const unsigned bytes = static_cast<unsigned>(cnt * sizeof(R));
-        const int nplanes = NV * NP;
-        const int ncopy = (a.mode == 4) ? nplanes : 2 * nplanes;
-        if (tid == 0) mbar_expect_tx(bar, bytes * ncopy);
-        __syncwarp();
-        for (int q = tid; q < ncopy; q += 32) {
-            // planes [0, nplanes): base state (modes 2, 3), then the accumulator;
-            // mode 4 copies only the accumulator, to planes [0, nplanes)
-            const int which = (a.mode == 4) ? 1 : (q >= nplanes);
-            const int pl = q % nplanes;
-            const R *src = static_cast<const R *>(which ? a.acc : a.c) + pl * SE + static_cast<size_t>(tile) * kTile;
-            bulk_copy_g2s(s_pre + static_cast<size_t>(q) * kTile, src, bytes, bar);
-        }
-    }
+    const bool pre = issue_prefetch<P, NV>(a, tile, bar, s_pre, tid);
 
     // own coefficients (coalesced: 32 consecutive elements per warp and (n,i))
     R c[NV][NP];
@@ -536,100 +656,10 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
             }
     }
 
-    // ---- mass inverse and RK combination ---------------------------------------
-    const R sc = dt * invJ;
-    R *__restrict__ out = static_cast<R *>(a.out);
-    const R *pc = nullptr, *pacc = nullptr;   // base state / accumulator of this element
-    size_t pstride = SE;
-    if (pre) {
-        if (!mbar_wait_bounded(bar, parity, 1ll << 26)) {
-            // the copies did not land in time: report, wait once more for the
-            // copies still in flight (they write this CTA's shared memory), skip
-            atomicOr(a.status, kStatusCopyTimeout);
-            mbar_wait_bounded(bar, parity, 1ll << 28);
-            return pre;
-        }
-        pc = s_pre + tid;
-        pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * kTile) + tid;
-        pstride = kTile;
-    } else {
-        pc = static_cast<const R *>(a.c) + e;
-        pacc = static_cast<const R *>(a.acc) + e;
-    }
-    switch (a.mode) {
-    case 0:
-#pragma unroll
-        for (int n = 0; n < NV; ++n)
-#pragma unroll
-            for (int i = 0; i < NP; ++i) out[(n * NP + i) * SE + e] = sc * rhs[n][i];
-        break;
-    case 1: {   // u2 = c + k1/2, acc = c + k1/6
-        R *__restrict__ acc = static_cast<R *>(a.acc);
-#pragma unroll
-        for (int n = 0; n < NV; ++n)
-#pragma unroll
-            for (int i = 0; i < NP; ++i) {
-                const R kk = sc * rhs[n][i];
-                const size_t o = (n * NP + i) * SE + e;
-                out[o] = fma(R(0.5), kk, c[n][i]);
-                acc[o] = fma(R(1.0 / 6.0), kk, c[n][i]);
-            }
-        break;
-    }
-    case 2:     // u3 = c + k2/2, acc += k2/3
-    case 3: {   // u4 = c + k3,   acc += k3/3
-        R *__restrict__ acc = static_cast<R *>(a.acc);
-        const R alpha = a.mode == 2 ? R(0.5) : R(1);
-#pragma unroll
-        for (int n = 0; n < NV; ++n)
-#pragma unroll
-            for (int i = 0; i < NP; ++i) {
-                const R kk = sc * rhs[n][i];
-                const size_t o = (n * NP + i) * SE + e;
-                const size_t po = (n * NP + i) * pstride;
-                out[o] = fma(alpha, kk, pc[po]);
-                acc[o] = fma(R(1.0 / 3.0), kk, pacc[po]);
-            }
-        break;
-    }
-    case 4: {   // c = acc + k4/6
-#pragma unroll
-        for (int n = 0; n < NV; ++n)
-#pragma unroll
-            for (int i = 0; i < NP; ++i) {
-                const size_t o = (n * NP + i) * SE + e;
-                out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], pacc[(n * NP + i) * pstride]);
-            }
-        break;
-    }
-    case 5: {   // out = u + alpha k (RK2 first stage, forward Euler)
-        const R alpha = R(a.alpha);
-#pragma unroll
-        for (int n = 0; n < NV; ++n)
-#pragma unroll
-            for (int i = 0; i < NP; ++i) out[(n * NP + i) * SE + e] = fma(alpha, sc * rhs[n][i], c[n][i]);
-        break;
-    }
-    default: {  // 6: out = c + alpha k (RK2 second stage).  out may be the base
-                // state itself: each thread reads and then writes only its own
-                // element's values, and no other thread reads them
-        const R alpha = R(a.alpha);
-        const R *pb = static_cast<const R *>(a.c) + e;
-        R *po = static_cast<R *>(a.out) + e;
-#pragma unroll
-        for (int n = 0; n < NV; ++n)
-#pragma unroll
-            for (int i = 0; i < NP; ++i) {
-                const size_t o = (n * NP + i) * SE;
-                const R base = pb[o];
-                po[o] = fma(alpha, sc * rhs[n][i], base);
-            }
-        break;
-    }
-    }
-    return pre;
+    return stage_epilogue<P, EQ>(a, rhs, c, dt, invJ, e, SE, pre, s_pre, bar, parity, tid);
 }
 
+#ifndef DGX_STAGE_NO_LAUNCHERS   // (a translation unit that needs only the device functions and tables)
 #ifndef DGX_MIN_CTAS_P3
 #define DGX_MIN_CTAS_P3 3
 #endif
@@ -769,6 +799,8 @@ static int launch_stage_impl(int order, int equation, const StageArgs &a, cudaSt
     return equation == DGX_EULER ? launch_order<DGX_EULER>(order, a, st)
                                  : launch_order<DGX_ADVECTION>(order, a, st);
 }
+
+#endif   // DGX_STAGE_NO_LAUNCHERS
 
 // Fill this translation unit's constant tables from the FP64 host tables.
 static int upload_tables_impl() {

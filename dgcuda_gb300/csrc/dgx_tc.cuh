@@ -88,6 +88,17 @@ __device__ __forceinline__ void tmem_st8(unsigned taddr, const unsigned *r) {
                  "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
                  : "memory");
 }
+__device__ __forceinline__ void tmem_st1(unsigned taddr, unsigned r0) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x1.b32 [%0], {%1};" ::"r"(taddr), "r"(r0) : "memory");
+}
+__device__ __forceinline__ void tmem_st2(unsigned taddr, unsigned r0, unsigned r1) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1,%2};" ::"r"(taddr), "r"(r0), "r"(r1) : "memory");
+}
+__device__ __forceinline__ void tmem_st4(unsigned taddr, const unsigned *r) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "r"(r[0]), "r"(r[1]),
+                 "r"(r[2]), "r"(r[3])
+                 : "memory");
+}
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // lane field of a tensor-memory address for this warp's 32x32b accesses
@@ -149,6 +160,15 @@ __device__ __forceinline__ unsigned pack_bf16(float a, float b) {
     unsigned r;
     asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
     return r;
+}
+// One value as the BF16 pair (hi, lo) in one 32-bit word, hi in the low half:
+// hi = bf16(x), lo = bf16(x - hi)
+__device__ __forceinline__ unsigned split_word(float x) {
+    unsigned h, w;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(0.0f), "f"(x));
+    const float r = x - __uint_as_float(h << 16);
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(w) : "f"(r), "f"(x));
+    return w;
 }
 __device__ __forceinline__ void split_bf16(float a, float b, unsigned &hi, unsigned &lo) {
     hi = pack_bf16(a, b);
