@@ -336,13 +336,15 @@ __device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, uns
 // 445-464, 622-700): k = dt/J rhs, then per mode of the kernel
 //   0 k;  1 u2 = c + k/2, acc = c + k/6;  2/3 u = c + alpha k, acc += k/3;
 //   4 c = acc + k/6;  5 out = u + alpha k;  6 out = c + alpha k.
-// Waits (bounded) for the tile's prefetched base state and accumulator when
-// `pre`; returns `pre`.
-template <int P, int EQ>
-__device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs)[(EQ == DGX_EULER) ? 4 : 1][num_modes(P)],
-                                               const R (&c)[(EQ == DGX_EULER) ? 4 : 1][num_modes(P)], R dt, R invJ,
+// Writes the variables V0 .. V0+VC-1 (all of them by default; rhs and c hold
+// just those).  Waits (bounded) for the tile's prefetched base state and
+// accumulator when `pre`; `row` is the element's index in the tile; returns
+// `pre`.
+template <int P, int EQ, int V0 = 0, int VC = (EQ == DGX_EULER) ? 4 : 1>
+__device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs)[VC][num_modes(P)],
+                                               const R (&c)[VC][num_modes(P)], R dt, R invJ,
                                                int e, size_t SE, bool pre, const R *s_pre,
-                                               unsigned long long *bar, unsigned parity, int tid) {
+                                               unsigned long long *bar, unsigned parity, int row) {
     constexpr int NP = num_modes(P);
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     const R sc = dt * invJ;
@@ -357,8 +359,8 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
             mbar_wait_bounded(bar, parity, 1ll << 28);
             return pre;
         }
-        pc = s_pre + tid;
-        pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * kTile) + tid;
+        pc = s_pre + row;
+        pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * kTile) + row;
         pstride = kTile;
     } else {
         pc = static_cast<const R *>(a.c) + e;
@@ -367,18 +369,18 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
     switch (a.mode) {
     case 0:
 #pragma unroll
-        for (int n = 0; n < NV; ++n)
+        for (int n = 0; n < VC; ++n)
 #pragma unroll
-            for (int i = 0; i < NP; ++i) out[(n * NP + i) * SE + e] = sc * rhs[n][i];
+            for (int i = 0; i < NP; ++i) out[((V0 + n) * NP + i) * SE + e] = sc * rhs[n][i];
         break;
     case 1: {   // u2 = c + k1/2, acc = c + k1/6
         R *__restrict__ acc = static_cast<R *>(a.acc);
 #pragma unroll
-        for (int n = 0; n < NV; ++n)
+        for (int n = 0; n < VC; ++n)
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
                 const R kk = sc * rhs[n][i];
-                const size_t o = (n * NP + i) * SE + e;
+                const size_t o = ((V0 + n) * NP + i) * SE + e;
                 out[o] = fma(R(0.5), kk, c[n][i]);
                 acc[o] = fma(R(1.0 / 6.0), kk, c[n][i]);
             }
@@ -389,12 +391,12 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
         R *__restrict__ acc = static_cast<R *>(a.acc);
         const R alpha = a.mode == 2 ? R(0.5) : R(1);
 #pragma unroll
-        for (int n = 0; n < NV; ++n)
+        for (int n = 0; n < VC; ++n)
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
                 const R kk = sc * rhs[n][i];
-                const size_t o = (n * NP + i) * SE + e;
-                const size_t po = (n * NP + i) * pstride;
+                const size_t o = ((V0 + n) * NP + i) * SE + e;
+                const size_t po = ((V0 + n) * NP + i) * pstride;
                 out[o] = fma(alpha, kk, pc[po]);
                 acc[o] = fma(R(1.0 / 3.0), kk, pacc[po]);
             }
@@ -402,20 +404,20 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
     }
     case 4: {   // c = acc + k4/6
 #pragma unroll
-        for (int n = 0; n < NV; ++n)
+        for (int n = 0; n < VC; ++n)
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
-                const size_t o = (n * NP + i) * SE + e;
-                out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], pacc[(n * NP + i) * pstride]);
+                const size_t o = ((V0 + n) * NP + i) * SE + e;
+                out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], pacc[((V0 + n) * NP + i) * pstride]);
             }
         break;
     }
     case 5: {   // out = u + alpha k (RK2 first stage, forward Euler)
         const R alpha = R(a.alpha);
 #pragma unroll
-        for (int n = 0; n < NV; ++n)
+        for (int n = 0; n < VC; ++n)
 #pragma unroll
-            for (int i = 0; i < NP; ++i) out[(n * NP + i) * SE + e] = fma(alpha, sc * rhs[n][i], c[n][i]);
+            for (int i = 0; i < NP; ++i) out[((V0 + n) * NP + i) * SE + e] = fma(alpha, sc * rhs[n][i], c[n][i]);
         break;
     }
     default: {  // 6: out = c + alpha k (RK2 second stage).  out may be the base
@@ -425,10 +427,10 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
         const R *pb = static_cast<const R *>(a.c) + e;
         R *po = static_cast<R *>(a.out) + e;
 #pragma unroll
-        for (int n = 0; n < NV; ++n)
+        for (int n = 0; n < VC; ++n)
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
-                const size_t o = (n * NP + i) * SE;
+                const size_t o = ((V0 + n) * NP + i) * SE;
                 const R base = pb[o];
                 po[o] = fma(alpha, sc * rhs[n][i], base);
             }

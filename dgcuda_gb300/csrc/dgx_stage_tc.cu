@@ -66,14 +66,20 @@ constexpr unsigned kStatusMmaTimeout = kStatusCopyTimeout;
 // size completes in microseconds)
 constexpr long long kMmaWait = 1ll << 22;
 
+constexpr int kTcThreads = 2 * kTile;   // two threads per element (row)
+
 template <int P, int EQ, bool BND>
-__global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
+__global__ void __launch_bounds__(kTcThreads, 2) stage_kernel_tc(const StageArgs a) {
     using L = Lay<P>;
     constexpr int NP = L::NP, NQ = L::NQ, NQ1 = L::NQ1;
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     using TC = TcCols<P, NV>;
     constexpr TcDims D = tc_dims(P);
     constexpr int TSW = slot_words<P, NV>();
+    // the two threads of a row split the variables (Euler: 0,1 | 2,3; advection:
+    // the first thread), the volume points and the side points
+    constexpr int VH = NV == 4 ? 2 : 1;
+    constexpr int QH = (NQ + 1) / 2, SP = 3 * NQ1, SH = (SP + 1) / 2;
 
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned long long *bar_pre = reinterpret_cast<unsigned long long *>(smem_raw);
@@ -94,28 +100,32 @@ __global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
         if (dt == R(0)) return;   // the run has reached its end time (uniform over the grid)
     }
     const int E = a.E;
-    const int tid = threadIdx.x;
-    const int e = tile * kTile + tid;
+    const int t = threadIdx.x;
+    const int r = t & (kTile - 1);    // row: element of the tile and tensor-memory lane
+    const int h = t / kTile;          // which of the row's two threads (uniform over a warp)
+    const int e = tile * kTile + r;
     const bool live = e < E;
     const size_t SE = static_cast<size_t>(E);
     const R g = R(a.gammaf), ax = R(a.axf), ay = R(a.ayf);
     const int llf = a.flux == DGX_FLUX_LLF;
     const R *__restrict__ u = static_cast<const R *>(a.u);
+    const bool has_vars = NV == 4 || h == 0;   // advection: the variable work is the first thread's
+    const int v0 = NV == 4 ? h * VH : 0;
 
-    if (tid == 0) {
+    if (t == 0) {
         mbar_init(bar_pre, 1);
         mbar_init(bar_mma, 1);
         *s_fail = 0;
     }
-    if (tid < 32) {
+    if (t < 32) {
         tc::tmem_alloc(s_tslot, TC::COLS);
         tc::tmem_relinquish();
     }
     {   // the constant B operands and the side tables (halo traces) into shared memory
         const uint4 *src = static_cast<const uint4 *>(a.tc_img);
         uint4 *dst = reinterpret_cast<uint4 *>(s_img);
-        for (int i = tid; i < D.bytes / 16; i += kTile) dst[i] = __ldg(src + i);
-        for (int t = tid; t < 3 * NP * NQ1; t += kTile) s_side[t] = c_tab[L::SIDE + t];
+        for (int i = t; i < D.bytes / 16; i += kTcThreads) dst[i] = __ldg(src + i);
+        for (int i = t; i < 3 * NP * NQ1; i += kTcThreads) s_side[i] = c_tab[L::SIDE + i];
     }
     tc::fence_before_sync();
     __syncthreads();   // barriers initialised, tensor memory allocated
@@ -123,14 +133,16 @@ __global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
     const unsigned tbase = *s_tslot;
     const unsigned tlane = tc::tmem_lane_base(tbase);
 
-    const bool pre = issue_prefetch<P, NV>(a, tile, bar_pre, s_pre, tid);
+    const bool pre = issue_prefetch<P, NV>(a, tile, bar_pre, s_pre, t);
 
-    // own coefficients, side data, geometry
-    R c[NV][NP];
+    // the row's mean coefficients, this thread's variables, side data, geometry
+    R c0[NV], cv[VH][NP];
 #pragma unroll
-    for (int n = 0; n < NV; ++n)
+    for (int n = 0; n < NV; ++n) c0[n] = live ? __ldg(u + (n * NP) * SE + e) : R(0);
 #pragma unroll
-        for (int i = 0; i < NP; ++i) c[n][i] = live ? __ldg(u + (n * NP + i) * SE + e) : R(0);
+    for (int n = 0; n < VH; ++n)
+#pragma unroll
+        for (int i = 0; i < NP; ++i) cv[n][i] = live && has_vars ? __ldg(u + ((v0 + n) * NP + i) * SE + e) : R(0);
     int sw[3];
     R snx[3], sny[3], shl[3];
     {
@@ -155,21 +167,24 @@ __global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
         ys = __ldg(geo + 4 * SE + e);
     }
 
-    // 1. A_U: modes 1..np-1 as (hi, lo) words, one column each; zero padding
+    // 1. A_U: modes 1..np-1 of this thread's variables as (hi, lo) words, one
+    //    column each; zero padding
+    if (has_vars) {
 #pragma unroll
-    for (int n = 0; n < NV; ++n) {
-        unsigned w[TC::AUW];
+        for (int n = 0; n < VH; ++n) {
+            unsigned w[TC::AUW];
 #pragma unroll
-        for (int m = 0; m < TC::AUW; ++m) w[m] = (m + 1 < NP) ? tc::split_word(c[n][m + 1]) : 0u;
+            for (int m = 0; m < TC::AUW; ++m) w[m] = (m + 1 < NP) ? tc::split_word(cv[n][m + 1]) : 0u;
 #pragma unroll
-        for (int b = 0; b < TC::AUW; b += 8) tc::tmem_st8(tlane + TC::AU + n * TC::AUW + b, w + b);
+            for (int b = 0; b < TC::AUW; b += 8) tc::tmem_st8(tlane + TC::AU + (v0 + n) * TC::AUW + b, w + b);
+        }
+        tc::tmem_wait_st();
     }
-    tc::tmem_wait_st();
     tc::fence_proxy_async();   // the B operands were written by the generic proxy
     tc::fence_before_sync();
     __syncthreads();
     // 2. D_U = A_U (B_U hi, hi) + A_U (B_U lo, lo)
-    if (tid == 0) {
+    if (t == 0) {
         tc::fence_after_sync();
         constexpr unsigned idu = tc::idesc_bf16_f32(kTile, D.nu);
         const unsigned sb = tc::smem_u32(s_img);
@@ -191,16 +206,16 @@ __global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
     {
         R ub[NV];
 #pragma unroll
-        for (int n = 0; n < NV; ++n) ub[n] = c[n][0] * phi0;
+        for (int n = 0; n < NV; ++n) ub[n] = c0[n] * phi0;
         phys_flux<EQ>(ub, g, ax, ay, fxr, fyr);
     }
 
     // halo traces (FP32), overlapping the MMAs: the tile's neighbours outside
     // the tile, on their own side and in their own point order
     {
-        const int h0 = __ldg(a.halo_off + tile), H = __ldg(a.halo_off + tile + 1) - h0;
-        for (int h = tid; h < H; h += kTile) {
-            const int hw = __ldg(a.halo_list + h0 + h);
+        const int hb = __ldg(a.halo_off + tile), H = __ldg(a.halo_off + tile + 1) - hb;
+        for (int hh = t; hh < H; hh += kTcThreads) {
+            const int hw = __ldg(a.halo_list + hb + hh);
             const int ne = hw >> 2;
             R cn[NV][NP];
 #pragma unroll
@@ -217,34 +232,43 @@ __global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
             for (int i = 0; i < NP; ++i)
 #pragma unroll
                 for (int j = 0; j < NQ1; ++j) {
-                    const R t = ts[i * NQ1 + j];
+                    const R tv = ts[i * NQ1 + j];
 #pragma unroll
-                    for (int n = 0; n < NV; ++n) tr[j][n] = fma(cn[n][i], t, tr[j][n]);
+                    for (int n = 0; n < NV; ++n) tr[j][n] = fma(cn[n][i], tv, tr[j][n]);
                 }
 #pragma unroll
             for (int j = 0; j < NQ1; ++j)
 #pragma unroll
-                for (int n = 0; n < NV; ++n) s_tr[(3 * kTile + h) * TSW + j * NV + n] = tr[j][n];
+                for (int n = 0; n < NV; ++n) s_tr[(3 * kTile + hh) * TSW + j * NV + n] = tr[j][n];
         }
     }
 
-    // 3. point values: volume points to registers, own traces to shared memory
+    // 3. point values: this thread's volume points to registers, its side
+    //    points (own traces) to shared memory
     if (!mbar_wait_bounded(bar_mma, 0, kMmaWait)) *s_fail = 1;
     tc::fence_after_sync();
-    R Uv[NV][NQ];
+    const int q0 = h * QH, s0 = h * SH;
+    R Uv[NV][QH];
 #pragma unroll
     for (int n = 0; n < NV; ++n) {
         float d[D.nu];
 #pragma unroll
         for (int b = 0; b < D.nu; b += 16) tc::tmem_ld16(tlane + TC::DU + n * D.nu + b, d + b);
         tc::tmem_wait_ld();
-        const R m0 = c[n][0] * phi0;
+        const R m0 = c0[n] * phi0;
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) Uv[n][q] = d[q] + m0;
+        for (int qq = 0; qq < QH; ++qq) {
+            // q0 + qq < NQ except for the second thread's last point at odd NQ
+            Uv[n][qq] = (h == 0 ? d[qq] : d[(QH + qq) < NQ ? QH + qq : 0]) + m0;
+        }
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
-#pragma unroll
-            for (int j = 0; j < NQ1; ++j) s_tr[(3 * tid + k) * TSW + j * NV + n] = d[NQ + k * NQ1 + j] + m0;
+        for (int ss = 0; ss < SH; ++ss) {
+            const int sp = s0 + ss;
+            if (sp < SP) {
+                const int k = sp / NQ1, j = sp - k * NQ1;
+                s_tr[(3 * r + k) * TSW + j * NV + n] = (h == 0 ? d[NQ + ss] : d[NQ + SH + ss < D.nu ? NQ + SH + ss : 0]) + m0;
+            }
+        }
     }
     __syncthreads();   // all traces of the tile and its halo are in shared memory
     const bool fail = *s_fail != 0;   // uniform over the CTA
@@ -255,45 +279,52 @@ __global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
         hxr[n] = fxr[n] * ys - fyr[n] * xs;
         hyr[n] = fyr[n] * xr - fxr[n] * yr;
     }
-    R sgk[3], frk[3][NV];   // per side: lift sign and length, reference normal flux
+    R sgk[3];             // per side: lift sign times half length
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int word = sw[k];
+        const bool bnd = BND && word < 0;
+        const int il = bnd ? 1 : (word & 1);
+        sgk[k] = il ? -shl[k] : shl[k];
+    }
     if (!fail) {
-        // A' volume part: (x part, y part) of the flux at point q, minus the reference
+        // A' volume part: (x part, y part) of the flux at this thread's points,
+        // minus the reference
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            R U[NV], fx[NV], fy[NV];
+        for (int qq = 0; qq < QH; ++qq) {
+            const int q = q0 + qq;
+            if (q < NQ) {
+                R U[NV], fx[NV], fy[NV];
 #pragma unroll
-            for (int n = 0; n < NV; ++n) U[n] = Uv[n][q];
-            phys_flux<EQ>(U, g, ax, ay, fx, fy);
+                for (int n = 0; n < NV; ++n) U[n] = Uv[n][qq];
+                phys_flux<EQ>(U, g, ax, ay, fx, fy);
 #pragma unroll
-            for (int n = 0; n < NV; ++n) {
-                const R hr = fx[n] * ys - fy[n] * xs - hxr[n];
-                const R hs = fy[n] * xr - fx[n] * yr - hyr[n];
-                tc::tmem_st2(tlane + TC::AP + n * TC::APW + 2 * q, tc::split_word(hr), tc::split_word(hs));
+                for (int n = 0; n < NV; ++n) {
+                    const R hr = fx[n] * ys - fy[n] * xs - hxr[n];
+                    const R hs = fy[n] * xr - fx[n] * yr - hyr[n];
+                    tc::tmem_st2(tlane + TC::AP + n * TC::APW + 2 * q, tc::split_word(hr), tc::split_word(hs));
+                }
             }
         }
-        // A' side part: the lifted numerical flux, minus the reference
+        // A' side part: the lifted numerical flux at this thread's side points,
+        // minus the reference
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const int word = pick3(sw[0], sw[1], sw[2], k);
-            const R nx = pick3(snx[0], snx[1], snx[2], k), ny = pick3(sny[0], sny[1], sny[2], k);
-            const R hl = pick3(shl[0], shl[1], shl[2], k);
-            const int own = 3 * tid + k;
-            const bool bnd = BND && word < 0;
-            const int slot = bnd ? own : (word >> 1);
-            const int il = bnd ? 1 : (word & 1);
-            const R *s_own = s_tr + own * TSW;
-            const R *s_nbr = s_tr + slot * TSW;
-            const R sg = il ? -hl : hl;
-            sgk[k] = sg;
-#pragma unroll
-            for (int n = 0; n < NV; ++n) frk[k][n] = fxr[n] * nx + fyr[n] * ny;
-#pragma unroll
-            for (int j = 0; j < NQ1; ++j) {
+        for (int ss = 0; ss < SH; ++ss) {
+            const int sp = s0 + ss;
+            if (sp < SP) {
+                const int k = sp / NQ1, j = sp - k * NQ1;
+                const int word = pick3(sw[0], sw[1], sw[2], k);
+                const R nx = pick3(snx[0], snx[1], snx[2], k), ny = pick3(sny[0], sny[1], sny[2], k);
+                const int own = 3 * r + k;
+                const bool bnd = BND && word < 0;
+                const int slot = bnd ? own : (word >> 1);
+                const int il = bnd ? 1 : (word & 1);
+                const R sg = pick3(sgk[0], sgk[1], sgk[2], k);
                 R UO[NV], UN[NV], UL[NV], UR[NV], Fh[NV];
 #pragma unroll
                 for (int n = 0; n < NV; ++n) {
-                    UO[n] = s_own[j * NV + n];
-                    UN[n] = s_nbr[(NQ1 - 1 - j) * NV + n];
+                    UO[n] = s_tr[own * TSW + j * NV + n];
+                    UN[n] = s_tr[slot * TSW + (NQ1 - 1 - j) * NV + n];
                 }
                 if constexpr (BND) {
                     if (bnd) boundary_ghost<P, EQ>(a, word, k, j, e, UO, nx, ny, UN);
@@ -306,21 +337,23 @@ __global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
                 num_flux<EQ>(UL, UR, nx, ny, llf, g, ax, ay, Fh);
 #pragma unroll
                 for (int n = 0; n < NV; ++n)
-                    tc::tmem_st1(tlane + TC::AP + n * TC::APW + 2 * NQ + k * NQ1 + j,
-                                 tc::split_word(sg * (Fh[n] - frk[k][n])));
+                    tc::tmem_st1(tlane + TC::AP + n * TC::APW + 2 * NQ + sp,
+                                 tc::split_word(sg * (Fh[n] - (fxr[n] * nx + fyr[n] * ny))));
             }
         }
         // zero padding of A'
+        if (h == 0) {
 #pragma unroll
-        for (int n = 0; n < NV; ++n)
+            for (int n = 0; n < NV; ++n)
 #pragma unroll
-            for (int col = D.ka; col < TC::APW; ++col) tc::tmem_st1(tlane + TC::AP + n * TC::APW + col, 0u);
+                for (int col = D.ka; col < TC::APW; ++col) tc::tmem_st1(tlane + TC::AP + n * TC::APW + col, 0u);
+        }
         tc::tmem_wait_st();
     }
     tc::fence_before_sync();
     __syncthreads();
     // 4. D_P = A' (B_P hi, hi) + A' (B_P lo, lo)
-    if (tid == 0 && !fail) {
+    if (t == 0 && !fail) {
         tc::fence_after_sync();
         constexpr unsigned idp = tc::idesc_bf16_f32(kTile, kTcNP);
         const unsigned sb = tc::smem_u32(s_img);
@@ -336,20 +369,30 @@ __global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
         tc::mma_commit(bar_mma);
     }
     bool ok = !fail;
-    R rhs[NV][NP];
+    R rhs[VH][NP];
     if (ok) {
-        // the reference state's part, exactly: its flux is constant over the
-        // element, so its projection is a constant times the tables' column sums
+        // the reference state's part of this thread's variables, exactly: its
+        // flux is constant over the element, so its projection is a constant
+        // times the tables' column sums
         const float *sums = reinterpret_cast<const float *>(s_img + D.off_sum);
 #pragma unroll
-        for (int n = 0; n < NV; ++n)
+        for (int n = 0; n < VH; ++n) {
+            const int v = v0 + n;
+            R hx = hxr[0], hy = hyr[0], fxv = fxr[0], fyv = fyr[0];
+#pragma unroll
+            for (int m = 1; m < NV; ++m)
+                if (v == m) { hx = hxr[m]; hy = hyr[m]; fxv = fxr[m]; fyv = fyr[m]; }
+            R fr[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) fr[k] = sgk[k] * (fxv * snx[k] + fyv * sny[k]);
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
-                R r = hxr[n] * sums[i] + hyr[n] * sums[16 + i];
+                R acc = hx * sums[i] + hy * sums[16 + i];
 #pragma unroll
-                for (int k = 0; k < 3; ++k) r = fma(sgk[k] * frk[k][n], sums[32 + 16 * k + i], r);
-                rhs[n][i] = r;
+                for (int k = 0; k < 3; ++k) acc = fma(fr[k], sums[32 + 16 * k + i], acc);
+                rhs[n][i] = acc;
             }
+        }
         if (!mbar_wait_bounded(bar_mma, 1, kMmaWait)) {
             atomicOr(a.status, kStatusMmaTimeout);
             mbar_wait_bounded(bar_mma, 1, 4 * kMmaWait);
@@ -357,9 +400,9 @@ __global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
         }
         tc::fence_after_sync();
 #pragma unroll
-        for (int n = 0; n < NV; ++n) {
+        for (int n = 0; n < VH; ++n) {
             float d[kTcNP];
-            tc::tmem_ld16(tlane + TC::DP + n * kTcNP, d);
+            tc::tmem_ld16(tlane + TC::DP + (v0 + n) * kTcNP, d);
             tc::tmem_wait_ld();
 #pragma unroll
             for (int i = 0; i < NP; ++i) rhs[n][i] += d[i];
@@ -367,18 +410,23 @@ __global__ void __launch_bounds__(kTile, 2) stage_kernel_tc(const StageArgs a) {
     } else {
         // the point-value MMAs did not complete in time: report, give them a
         // last chance before the tensor memory is freed, write nothing
-        if (tid == 0) atomicOr(a.status, kStatusMmaTimeout);
+        if (t == 0) atomicOr(a.status, kStatusMmaTimeout);
         mbar_wait_bounded(bar_mma, 0, 4 * kMmaWait);
     }
-    // 5. the RK combination
-    if (ok && live) {
-        stage_epilogue<P, EQ>(a, rhs, c, dt, invJ, e, SE, pre, s_pre, bar_pre, 0u, tid);
-    } else if (pre && tid < 32) {
+    // 5. the RK combination of this thread's variables
+    if (ok && live && has_vars) {
+        if constexpr (NV == 4) {
+            if (h == 0) stage_epilogue<P, EQ, 0, VH>(a, rhs, cv, dt, invJ, e, SE, pre, s_pre, bar_pre, 0u, r);
+            else stage_epilogue<P, EQ, VH, VH>(a, rhs, cv, dt, invJ, e, SE, pre, s_pre, bar_pre, 0u, r);
+        } else {
+            stage_epilogue<P, EQ, 0, VH>(a, rhs, cv, dt, invJ, e, SE, pre, s_pre, bar_pre, 0u, r);
+        }
+    } else if (pre && t < 32) {
         mbar_wait_bounded(bar_pre, 0u, 1ll << 28);   // no copy in flight at exit
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (tid < 32) tc::tmem_dealloc(tbase, TC::COLS);
+    if (t < 32) tc::tmem_dealloc(tbase, TC::COLS);
 }
 
 template <int P, int EQ, bool BND>
@@ -397,7 +445,7 @@ int launch_tc_one(const StageArgs &a_in, cudaStream_t st) {
         configured = smem;
     }
     const int grid = (a.E + kTile - 1) / kTile;
-    if (grid > 0) stage_kernel_tc<P, EQ, BND><<<grid, kTile, smem, st>>>(a);
+    if (grid > 0) stage_kernel_tc<P, EQ, BND><<<grid, kTcThreads, smem, st>>>(a);
     DGX_CHECK_LAUNCH();
     return DGX_OK;
 }
