@@ -21,7 +21,7 @@ FLUX_CENTRAL, FLUX_LLF = 0, 1
 FP32, FP32_BF16X3, FP64 = 0, 1, 2
 RK4, RK2, FE = 0, 1, 2
 DT_FIXED, DT_CFL = 0, 1
-OPT_PREFETCH, OPT_STAGE_TIME = 1, 2
+OPT_PREFETCH, OPT_STAGE_TIME, OPT_LIMITER = 1, 2, 3
 STAGE_TIME_EXACT, STAGE_TIME_REFERENCE = 0, 1
 BC_NONE, BC_FREESTREAM, BC_EXACT, BC_PROBLEM = 0, 1, 2, 3
 IC_GAUSSIAN, IC_POLY, IC_DENSITY_WAVE, IC_VORTEX, IC_CONSTANT = 0, 1, 2, 3, 4
@@ -101,6 +101,9 @@ SIGNATURES = {
     "dgx_max_wave_speed": (None, [_vp, _dp, _vp]),
     "dgx_launch_count": (None, [_vp, C.POINTER(C.c_longlong)]),
     "dgx_tc_selftest": (None, [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), _vp]),
+    "dgx_limit": (None, [_vp, _vp]),
+    "dgx_state_change": (None, [_vp, _vp, _dp, _vp]),
+    "dgx_run_steady": (None, [_vp, _d, _i, _ip, _dp, _vp]),
     "dgx_solver_set_option": (None, [_vp, _i, _i]),
     "dgx_solver_set_boundary": (None, [_vp, _i, _i, _dp]),
     "dgx_batch_create": (None, [C.POINTER(_vp), _i, C.POINTER(_vp)]),

@@ -142,7 +142,22 @@ int stage_launch(dgx_solver *sv, int mode, const void *u, const void *c, void *a
     return rc;
 }
 
+int run_stage_raw(dgx_solver *sv, int stage, cudaStream_t st);
+
+// One stage, then (DGX_OPT_LIMITER) the limiter on the state the stage wrote
 int run_stage(dgx_solver *sv, int stage, cudaStream_t st) {
+    int rc = run_stage_raw(sv, stage, st);
+    SolverDev &s = sv->s;
+    if (rc || !s.limiter) return rc;
+    void *out = s.c;
+    if (s.integrator == DGX_RK4 && stage < 3) out = stage == 1 ? s.ub : s.ua;
+    else if (s.integrator == DGX_RK2 && stage == 0) out = s.ua;
+    rc = limit_state(s, sv->mesh->d, out, st);
+    if (!rc) sv->launches++;
+    return rc;
+}
+
+int run_stage_raw(dgx_solver *sv, int stage, cudaStream_t st) {
     SolverDev &s = sv->s;
     int rc;
     const int nst = num_stages(s.integrator);
@@ -459,6 +474,7 @@ int dgx_solver_create(dgx_mesh *mesh, const dgx_solver_desc *desc, dgx_solver **
     if (!rc) rc = dalloc(&s.counter, 1, &acct);
     if (!rc) rc = dalloc(&s.status, 1, &acct);
     if (!rc) rc = dalloc(&s.steps, 1, &acct);
+    if (!rc) rc = dalloc(&s.chg_bits, 1, &acct);
     s.c = bufs[0]; s.ua = bufs[1]; s.acc = bufs[2]; s.ub = bufs[3];
     if (!rc) {
         const double init[8] = {0.0, 0.0, 0.0, 0.0, 0.7, 0.0, 0.0, 0.0};
@@ -485,7 +501,7 @@ int dgx_solver_create(dgx_mesh *mesh, const dgx_solver_desc *desc, dgx_solver **
 int dgx_solver_destroy(dgx_solver *sv) {
     if (!sv) return DGX_ERR_INVALID;
     SolverDev &s = sv->s;
-    void *ptrs[] = {s.c, s.acc, s.ua, s.ub, s.scal, s.lam_bits, s.counter, s.status, s.steps};
+    void *ptrs[] = {s.c, s.acc, s.ua, s.ub, s.scal, s.lam_bits, s.counter, s.status, s.steps, s.chg_bits, s.prev};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (sv->mesh) mesh_release(sv->mesh);
@@ -720,6 +736,10 @@ int dgx_solver_set_option(dgx_solver *sv, int option, int value) {
     if (!sv) return DGX_ERR_INVALID;
     switch (option) {
     case DGX_OPT_PREFETCH: sv->s.prefetch = value ? 1 : 0; return DGX_OK;
+    case DGX_OPT_LIMITER:
+        if (value && sv->s.order != 1) { set_error("the limiter serves p = 1"); return DGX_ERR_UNSUPPORTED; }
+        sv->s.limiter = value ? 1 : 0;
+        return DGX_OK;
     case DGX_OPT_STAGE_TIME:
         if (value != DGX_STAGE_TIME_EXACT && value != DGX_STAGE_TIME_REFERENCE) {
             set_error("unknown stage-time rule %d", value);
@@ -729,6 +749,53 @@ int dgx_solver_set_option(dgx_solver *sv, int option, int value) {
         return DGX_OK;
     default: set_error("unknown option %d", option); return DGX_ERR_INVALID;
     }
+}
+
+int dgx_limit(dgx_solver *sv, void *stream) {
+    if (!sv) return DGX_ERR_INVALID;
+    if (sv->s.order != 1) { set_error("the limiter serves p = 1"); return DGX_ERR_UNSUPPORTED; }
+    const int rc = limit_state(sv->s, sv->mesh->d, sv->s.c, as_stream(stream));
+    if (!rc) sv->launches++;
+    return rc;
+}
+
+int dgx_state_change(dgx_solver *sv, const void *prev, double *max_change, void *stream) {
+    if (!sv || !prev || !max_change) return DGX_ERR_INVALID;
+    const int rc = state_change(sv->s, prev, max_change, as_stream(stream));
+    if (!rc) sv->launches++;
+    return rc;
+}
+
+int dgx_run_steady(dgx_solver *sv, double tol, int max_steps, int *steps, double *change, void *stream) {
+    if (!sv || !(tol >= 0.0) || max_steps <= 0) { set_error("need tol >= 0 and max_steps > 0"); return DGX_ERR_INVALID; }
+    SolverDev &s = sv->s;
+    cudaStream_t st = as_stream(stream);
+    const size_t bytes = s.n * elem_size(s);
+    if (!s.prev) {
+        char *p = nullptr;
+        int rc = dalloc(&p, bytes, &sv->device_bytes);
+        if (rc) return rc;
+        s.prev = p;
+    }
+    double chg = INFINITY;
+    int n = 0;
+    while (n < max_steps) {
+        DGX_TRY_CUDA(cudaMemcpyAsync(s.prev, s.c, bytes, cudaMemcpyDeviceToDevice, st));
+        int rc = dgx_step(sv, stream);
+        if (rc) return rc;
+        ++n;
+        rc = state_change(s, s.prev, &chg, st);
+        if (rc) return rc;
+        sv->launches++;
+        unsigned status = 0;
+        DGX_TRY_CUDA(cudaMemcpy(&status, s.status, sizeof(status), cudaMemcpyDeviceToHost));
+        if (status & kStatusCopyTimeout) { set_error("a bounded wait for an asynchronous copy ran out"); return DGX_ERR_TIMEOUT; }
+        if (status) { set_error("state became non-finite or unphysical (flags %u)", status); return DGX_ERR_NONFINITE; }
+        if (chg <= tol) break;
+    }
+    if (steps) *steps = n;
+    if (change) *change = chg;
+    return DGX_OK;
 }
 
 int dgx_max_wave_speed(dgx_solver *sv, double *out, void *stream) {

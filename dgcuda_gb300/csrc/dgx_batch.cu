@@ -225,6 +225,11 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
             batch_free(b);
             return DGX_ERR_UNSUPPORTED;
         }
+        if (solvers[i]->s.limiter) {
+            set_error("solver %d: batches do not apply the limiter", i);
+            batch_free(b);
+            return DGX_ERR_UNSUPPORTED;
+        }
         if (solvers[i]->s.integrator != DGX_RK4) {
             set_error("solver %d: batches take RK4 solvers only", i);
             batch_free(b);

@@ -105,6 +105,9 @@ struct SolverDev {
     int integrator = DGX_RK4;          // dgx_integrator
     int stage_time = DGX_STAGE_TIME_EXACT;   // DGX_OPT_STAGE_TIME
     int prefetch = 1;                  // DGX_OPT_PREFETCH
+    int limiter = 0;                   // DGX_OPT_LIMITER: limit every stage's output (p = 1)
+    unsigned long long *chg_bits = nullptr;   // largest coefficient change (double bits)
+    void *prev = nullptr;              // dgx_run_steady: the state before the step (on demand)
     int bc_kind = 0, bc_ic = 0;        // boundary ghost states (StageArgs)
     double bc_state[4] = {0, 0, 0, 0};
     double bc_params[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -226,6 +229,10 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
 int mesh_geometry(MeshDev &m, cudaStream_t st);
 int project_ic(const SolverDev &s, const MeshDev &m, int ic, const double *params, cudaStream_t st);
 int launch_dt(SolverDev &s, const MeshDev &m, cudaStream_t st);
+// the p = 1 slope limiter on a state vector in place, and the largest
+// |c - prev| over the state (FP64, synchronous) (dgx_limit.cu)
+int limit_state(const SolverDev &s, const MeshDev &m, void *state, cudaStream_t st);
+int state_change(const SolverDev &s, const void *prev, double *out, cudaStream_t st);
 // dst = src (whole state vectors) when the current step advanced (dt != 0)
 int commit_state(const SolverDev &s, void *dst, const void *src, cudaStream_t st);
 // stages per step of an integrator

@@ -207,6 +207,19 @@ class Solver:
         P[:len(params)] = params
         call("dgx_solver_set_boundary", self.h, int(kind), int(ic), _dp(P))
 
+    def limit(self, stream: int = 0) -> None:
+        call("dgx_limit", self.h, stream)
+
+    def state_change(self, prev_ptr: int, stream: int = 0) -> float:
+        v = C.c_double()
+        call("dgx_state_change", self.h, prev_ptr, C.byref(v), stream)
+        return v.value
+
+    def run_steady(self, tol: float, max_steps: int, stream: int = 0):
+        n, chg = C.c_int(), C.c_double()
+        call("dgx_run_steady", self.h, float(tol), int(max_steps), C.byref(n), C.byref(chg), stream)
+        return n.value, chg.value
+
     def set_option(self, option: int, value: int) -> None:
         call("dgx_solver_set_option", self.h, int(option), int(value))
 

@@ -217,6 +217,29 @@ int dgx_conserved_totals(dgx_solver *solver, double *out, void *stream);
 #define DGX_TOTALS_STATIC_MAX_ELEMS 16777216
 int dgx_conserved_totals_static(const dgx_solver *solver, const void *state, double *out,
                                 void *stream);
+/* Slope limiter for p = 1 on the resident state, in place (the reference's
+ * "standard limiter for p = 1", limit_c, src/2d/conservation/conserv_kernels.cu:
+ * 522-621, which its integrator leaves disabled and whose bounds it never
+ * sets), in Barth-Jespersen form: per element and variable the two linear
+ * modes are scaled by the largest phi <= 1 that keeps the traces at the side
+ * Gauss points within the range of the cell averages of the element and its
+ * three neighbours (a boundary side contributes the element itself).  Cell
+ * averages are unchanged.  Asynchronous on `stream`; other orders:
+ * DGX_ERR_UNSUPPORTED. */
+int dgx_limit(dgx_solver *solver, void *stream);
+/* Largest |c - prev| over every coefficient of the resident state, in FP64
+ * (prev: a device state in the solver's layout and precision), the quantity
+ * of the reference's disabled steady-state test (check_convergence,
+ * conserv_kernels.cu:943-947, time_integrator.cu:401-421).  Synchronous. */
+int dgx_state_change(dgx_solver *solver, const void *prev, double *max_change, void *stream);
+/* Step until the largest coefficient change of one step is <= tol, or
+ * max_steps steps (the reference's `while (t < endtime && convergence > TOL)`
+ * loop with TOL = 5e-8, time_integrator.cu:247-251).  Keeps one more state
+ * vector on the device (allocated on the first call).  Returns the steps taken
+ * and the last step's change.  The end time still applies: at it, dt = 0 and
+ * the change is 0. */
+int dgx_run_steady(dgx_solver *solver, double tol, int max_steps, int *steps, double *change,
+                   void *stream);
 /* Maximum cell-average wave speed of the resident state. */
 int dgx_max_wave_speed(dgx_solver *solver, double *out, void *stream);
 /* Vertex values of every variable as the reference's Gmsh "ST" views
@@ -263,7 +286,11 @@ int dgx_solver_set_boundary(dgx_solver *solver, int kind, int ic, const double *
  *                       (time_integrator.cu:733, src/2d/time_integrator.cu:145).
  *                     Periodic meshes and time-independent boundary data give
  *                     the same results under both. */
-enum dgx_option { DGX_OPT_PREFETCH = 1, DGX_OPT_STAGE_TIME = 2 };
+/*   DGX_OPT_LIMITER   1: apply dgx_limit to the state every stage writes (the
+ *                     reference's limiter hook after each stage,
+ *                     time_integrator.cu:302,332,363); p = 1 only, single
+ *                     solves (batches refuse such solvers); 0 (default): off. */
+enum dgx_option { DGX_OPT_PREFETCH = 1, DGX_OPT_STAGE_TIME = 2, DGX_OPT_LIMITER = 3 };
 enum dgx_stage_time { DGX_STAGE_TIME_EXACT = 0, DGX_STAGE_TIME_REFERENCE = 1 };
 int dgx_solver_set_option(dgx_solver *solver, int option, int value);
 /* Number of CUDA kernels this solver has launched so far. */

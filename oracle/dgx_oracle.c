@@ -297,6 +297,7 @@ typedef struct {
     int bc_kind, bc_ic;
     int integrator;       /* 0 RK4, 1 RK2 midpoint, 2 forward Euler */
     int ref_time;         /* 1: the reference's stage-time arguments */
+    int limiter;          /* 1: orc_limit_p1 on every stage's output state */
     double bc_state[4], bc_params[8];
 } orc_solver;
 
@@ -727,6 +728,55 @@ static double orc_stage_time(const orc_solver *S, double t, double dt, double no
     return t;
 }
 
+/* p = 1 slope limiter in place, Barth-Jespersen form of the reference's
+ * limit_c (conserv_kernels.cu:522-621; its bounds umin/umax are never set and
+ * its calls are commented out, time_integrator.cu:302,332,363): per element
+ * and variable, the linear modes are scaled by min over the 6 side Gauss
+ * points of min(1, (M - u0)/(u_j - u0)) (u_j > u0) or min(1, (m - u0)/(u_j -
+ * u0)) (u_j < u0), m/M the extremes of the cell averages of the element and
+ * its neighbours (a boundary side: the element itself). */
+int orc_limit_p1(const orc_solver *S, double *c) {
+    const orc_tables *T = &S->T;
+    int E = S->num_elem, e;
+    if (T->p != 1) return -1;
+#pragma omp parallel for schedule(static)
+    for (e = 0; e < E; e++) {
+        int nb[3], k, n, j;
+        for (k = 0; k < 3; k++) {
+            int s = S->elem_s[k][e], le = S->left_elem[s], re = S->right_elem[s];
+            int other = le == e ? re : le;
+            nb[k] = other >= 0 ? other : e;
+        }
+        for (n = 0; n < S->nv; n++) {
+            double *cn = c + (size_t)n * 3 * E;
+            double c0 = cn[e], c1 = cn[E + e], c2 = cn[2 * E + e];
+            double u0 = c0 * T->phi[0], lo = u0, hi = u0, phi = 1.0;
+            for (k = 0; k < 3; k++) {
+                double un = cn[nb[k]] * T->phi[0];
+                lo = fmin(lo, un);
+                hi = fmax(hi, un);
+            }
+            for (k = 0; k < 3; k++)
+                for (j = 0; j < 2; j++) {
+                    double uj = c0 * T->side[(k * 3 + 0) * 2 + j] + c1 * T->side[(k * 3 + 1) * 2 + j] +
+                                c2 * T->side[(k * 3 + 2) * 2 + j];
+                    double d = uj - u0, pj = 1.0;
+                    if (d > 0.0) pj = fmin(1.0, (hi - u0) / d);
+                    else if (d < 0.0) pj = fmin(1.0, (lo - u0) / d);
+                    phi = fmin(phi, pj);
+                }
+            if (phi < 1.0) { cn[E + e] = c1 * phi; cn[2 * E + e] = c2 * phi; }
+        }
+    }
+    return 0;
+}
+
+int orc_set_limiter(orc_solver *S, int on) {
+    if (on && S->T.p != 1) return -1;
+    S->limiter = on ? 1 : 0;
+    return 0;
+}
+
 /* one classic RK4 step in the reference's form (time_integrator.cu:276-398) */
 int orc_rk4_step(orc_solver *S, double *c, double dt, double t) {
     size_t N = (size_t)S->nv * S->T.np * S->num_elem, i;
@@ -742,6 +792,7 @@ int orc_rk4_step(orc_solver *S, double *c, double dt, double t) {
             double *ks = S->kstar, *kk = S->k[st];
 #pragma omp parallel for schedule(static)
             for (i = 0; i < N; i++) ks[i] = c[i] + a * kk[i];
+            if (S->limiter) orc_limit_p1(S, S->kstar);
             src = S->kstar;
         }
     }
@@ -750,6 +801,7 @@ int orc_rk4_step(orc_solver *S, double *c, double dt, double t) {
 #pragma omp parallel for schedule(static)
         for (i = 0; i < N; i++) c[i] += k1[i] / 6. + k2[i] / 3. + k3[i] / 3. + k4[i] / 6.;
     }
+    if (S->limiter) orc_limit_p1(S, c);
     return 0;
 }
 
@@ -765,6 +817,7 @@ int orc_rk2_step(orc_solver *S, double *c, double dt, double t) {
 #pragma omp parallel for schedule(static)
         for (i = 0; i < N; i++) ks[i] = c[i] + 0.5 * k1[i];
     }
+    if (S->limiter) orc_limit_p1(S, S->kstar);
     rc = orc_rhs(S, S->kstar, S->k[1], dt, orc_stage_time(S, t, dt, 0.5));
     if (rc) return rc;
     {
@@ -772,6 +825,7 @@ int orc_rk2_step(orc_solver *S, double *c, double dt, double t) {
 #pragma omp parallel for schedule(static)
         for (i = 0; i < N; i++) c[i] += k2[i];
     }
+    if (S->limiter) orc_limit_p1(S, c);
     return 0;
 }
 
@@ -786,6 +840,7 @@ int orc_fe_step(orc_solver *S, double *c, double dt, double t) {
 #pragma omp parallel for schedule(static)
         for (i = 0; i < N; i++) c[i] += k1[i];
     }
+    if (S->limiter) orc_limit_p1(S, c);
     return 0;
 }
 

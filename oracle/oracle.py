@@ -66,6 +66,8 @@ def lib():
         L.orc_rk4_step.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
         L.orc_step.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double]
         L.orc_set_integrator.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.orc_limit_p1.argtypes = [C.c_void_p, _dp]
+        L.orc_set_limiter.argtypes = [C.c_void_p, C.c_int]
         L.orc_run.argtypes = [C.c_void_p, _dp, C.c_int, C.c_double, C.c_double, C.c_double,
                               C.c_int, C.POINTER(C.c_double)]
         L.orc_totals.argtypes = [C.c_void_p, _dp, _dp]
@@ -170,6 +172,18 @@ class Oracle:
         reference's stage-time arguments for time-dependent boundary data."""
         if lib().orc_set_integrator(self.h, int(integrator), int(bool(reference_stage_time))):
             raise ValueError(f"unknown integrator {integrator}")
+
+    def limit(self, c) -> np.ndarray:
+        """The p = 1 slope limiter applied to a copy of c."""
+        c = self._state(c).copy()
+        if lib().orc_limit_p1(self.h, c):
+            raise ValueError("the limiter serves p = 1")
+        return c
+
+    def set_limiter(self, on: bool) -> None:
+        """Apply the limiter to every stage's output state (p = 1)."""
+        if lib().orc_set_limiter(self.h, int(bool(on))):
+            raise ValueError("the limiter serves p = 1")
 
     def max_lambda(self, c) -> float:
         return lib().orc_max_lambda(self.h, self._state(c))
