@@ -214,9 +214,14 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
     a.gammaf = static_cast<float>(s.gamma);
     a.axf = static_cast<float>(s.ax);
     a.ayf = static_cast<float>(s.ay);
-    // plane starts are 16-byte aligned when E * sizeof(value) is a multiple of 16
-    a.prefetch = s.prefetch && (static_cast<size_t>(m.num_elem) * elem_size(s)) % 16 == 0 &&
-                 mode >= 2 && mode <= 4 && c && acc;
+    // the epilogue operands of stages 2-4 are the solver's own buffers (16-byte
+    // slack at their end for the widened prefetch slices)
+    if (s.prefetch && mode >= 2 && mode <= 4 && c && acc) {
+        const int align = 16 / static_cast<int>(elem_size(s));   // values per 16 bytes
+        a.prefetch = m.num_elem % align == 0 ? kTile : kTile + align;
+    } else {
+        a.prefetch = 0;
+    }
     a.status = s.status;
     a.u = u;
     a.c = c;
@@ -468,7 +473,8 @@ int dgx_solver_create(dgx_mesh *mesh, const dgx_solver_desc *desc, dgx_solver **
     // c and ua for every integrator; RK4 adds its accumulator and a second stage input
     char *bufs[4] = {nullptr, nullptr, nullptr, nullptr};
     const int nbuf = s.integrator == DGX_RK4 ? 4 : 2;
-    for (int i = 0; i < nbuf && !rc; ++i) rc = dalloc(&bufs[i], s.n * es, &acct);
+    // 64 bytes of slack: the epilogue prefetch widens each slice to 16-byte boundaries
+    for (int i = 0; i < nbuf && !rc; ++i) rc = dalloc(&bufs[i], s.n * es + 64, &acct);
     if (!rc) rc = dalloc(&s.scal, 8, &acct);
     if (!rc) rc = dalloc(&s.lam_bits, 1, &acct);
     if (!rc) rc = dalloc(&s.counter, 1, &acct);

@@ -29,6 +29,7 @@ struct BatchClass {
     int n_items = 0;
     int nslot = 0;
     int prefetch = 1;                        // tuned option
+    int pre_plane = 0;                       // values per prefetched plane (largest of the solves)
     int persistent = 0;                      // tuned option: 0 flat grid, k > 0: k CTAs per SM
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
@@ -80,7 +81,7 @@ int class_launch(dgx_batch *b, BatchClass &k, int stage, cudaStream_t st) {
     a.items = k.d_items;
     a.n_items = k.n_items;
     a.nslot = k.nslot;
-    a.prefetch = stage >= 1 ? k.prefetch : 0;
+    a.prefetch = (stage >= 1 && k.prefetch) ? k.pre_plane : 0;
     a.bnd = k.bnd;
     if (k.persistent > 0) a.grid = std::min(k.n_items, num_sms() * k.persistent);
     else a.grid = k.n_items;
@@ -92,7 +93,7 @@ int class_launch(dgx_batch *b, BatchClass &k, int stage, cudaStream_t st) {
 // Upload the per-solve stage arguments of one class for the given options.
 int class_upload(dgx_batch *b, BatchClass &k) {
     std::vector<StageArgs> host(k.solves.size());
-    int nslot = 0;
+    int nslot = 0, plane = 0;
     for (int stage = 0; stage < 4; ++stage) {
         for (size_t j = 0; j < k.solves.size(); ++j) {
             dgx_solver *sv = b->solvers[k.solves[j]];
@@ -107,20 +108,23 @@ int class_upload(dgx_batch *b, BatchClass &k) {
             }
             s.prefetch = saved;
             nslot = std::max(nslot, host[j].nslot);
+            plane = std::max(plane, host[j].prefetch);
         }
         DGX_TRY_CUDA(cudaMemcpy(k.d_args[stage], host.data(), host.size() * sizeof(StageArgs),
                                 cudaMemcpyHostToDevice));
     }
     k.nslot = nslot;
+    k.pre_plane = plane;
     // refuse a prefetch that would not fit in shared memory
-    const size_t smem = k.precision == DGX_FP64 ? batch_smem_f64(k.order, k.equation, nslot, k.prefetch)
-                                                : batch_smem_f32(k.order, k.equation, nslot, k.prefetch);
+    const int pp = k.prefetch ? k.pre_plane : 0;
+    const size_t smem = k.precision == DGX_FP64 ? batch_smem_f64(k.order, k.equation, nslot, pp)
+                                                : batch_smem_f32(k.order, k.equation, nslot, pp);
     if (k.prefetch && smem > 200 * 1024) {
         k.prefetch = 0;
         return class_upload(b, k);
     }
     // set the kernel's shared-memory limit outside any capture (grid 0: no launch)
-    BatchStageArgs probe{k.d_args[1], k.d_items, 0, 0, k.nslot, k.prefetch, k.bnd};
+    BatchStageArgs probe{k.d_args[1], k.d_items, 0, 0, k.nslot, pp, k.bnd};
     int rc = launch_batch_stage(k.precision, k.order, k.equation, probe, nullptr);
     return rc;
 }

@@ -139,7 +139,7 @@ struct StageArgs {
     int flux;
     double gamma, ax, ay;
     float gammaf, axf, ayf;   // the same in FP32 (FP32 kernels)
-    int prefetch;      // 1: copy the epilogue operands with the TMA engine (needs 16-byte aligned planes)
+    int prefetch;      // > 0: copy the epilogue operands with the TMA engine, this many values per plane
     unsigned int *status;
     const void *u;     // stage input (read-only)
     const void *c;     // base state
@@ -173,7 +173,7 @@ struct BatchStageArgs {
     int n_items;
     int grid;
     int nslot;               // largest nslot of the class (shared-memory size)
-    int prefetch;            // any solve of the class prefetches
+    int prefetch;            // values per prefetched plane, the largest of the class's solves (0: none)
     int bnd;                 // any solve of the class has boundary sides
 };
 
@@ -186,8 +186,8 @@ int launch_batch_stage_f32_nb(int order, int equation, const BatchStageArgs &b, 
 int launch_batch_stage_f32_b(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
 int launch_batch_stage_f64_nb(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
 int launch_batch_stage_f64_b(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
-size_t batch_smem_f32(int order, int equation, int nslot, int prefetch);
-size_t batch_smem_f64(int order, int equation, int nslot, int prefetch);
+size_t batch_smem_f32(int order, int equation, int nslot, int prefetch_plane);
+size_t batch_smem_f64(int order, int equation, int nslot, int prefetch_plane);
 // the BF16x3 tensor-core kernels (dgx_stage_tc.cu) and their tables
 int launch_stage_tc(int order, int equation, const StageArgs &a, cudaStream_t st);
 int upload_tables_tc();

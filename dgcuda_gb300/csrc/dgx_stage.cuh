@@ -281,18 +281,23 @@ DGX_HD constexpr int side_table_words() { return (3 * num_modes(P) * num_quad1(P
 template <int P, int NV>
 DGX_HD constexpr int slot_words() { return (NV * num_quad1(P)) | 1; }
 
-// bytes of the prefetched epilogue operands (base state and accumulator slices
-// of the tile: 2 x NV x NP planes of kTile values)
+// Prefetched epilogue operands: per plane (variable x mode) of the base state
+// and of the accumulator, the tile's slice, widened to 16-byte boundaries (the
+// bulk copy needs 16-byte aligned ends, and a plane of E values starts on one
+// only when E is a multiple of kPreAlign).  StageArgs::prefetch holds the
+// values per plane in shared memory: kTile when E is a multiple of kPreAlign,
+// kTile + kPreAlign otherwise (0: no prefetch).
+constexpr int kPreAlign = 16 / static_cast<int>(sizeof(R));
 template <int P, int NV>
-DGX_HD constexpr size_t prefetch_bytes() {
-    return sizeof(R) * 2 * NV * num_modes(P) * kTile;
+DGX_HD constexpr size_t prefetch_bytes(int plane) {
+    return sizeof(R) * 2 * NV * num_modes(P) * static_cast<size_t>(plane);
 }
 
 template <int P, int NV>
 DGX_HD constexpr size_t stage_smem_bytes(int nslot, int prefetch) {
     return 16 + sizeof(R) * (static_cast<size_t>(side_table_words<P, NV>()) +
                              static_cast<size_t>(slot_words<P, NV>()) * nslot) +
-           (prefetch ? prefetch_bytes<P, NV>() : 0);
+           prefetch_bytes<P, NV>(prefetch);
 }
 
 // One tile of one solve.  `bar` is an initialised mbarrier; `parity` the phase
@@ -314,18 +319,30 @@ __device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, uns
         // (a previous tile) before the bulk copies that overwrite it
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         const int cnt = min(kTile, E - tile * kTile);
-        const unsigned bytes = static_cast<unsigned>(cnt * sizeof(R));
         const int nplanes = NV * NP;
         const int ncopy = (a.mode == 4) ? nplanes : 2 * nplanes;
-        if (tid == 0) mbar_expect_tx(bar, bytes * ncopy);
+        // plane pl's slice [g0, g0 + cnt) widened to [g0 & -A, (g0 + cnt + A-1) & -A)
+        // (the state buffers carry 16 bytes of slack past their end)
+        const size_t A = kPreAlign;
+        if (tid == 0) {
+            unsigned total = 0;
+            for (int pl = 0; pl < nplanes; ++pl) {
+                const size_t g0 = pl * SE + static_cast<size_t>(tile) * kTile;
+                total += static_cast<unsigned>((((g0 + cnt + A - 1) & ~(A - 1)) - (g0 & ~(A - 1))) * sizeof(R));
+            }
+            mbar_expect_tx(bar, total * (ncopy / nplanes));
+        }
         __syncwarp();
         for (int q = tid; q < ncopy; q += 32) {
             // planes [0, nplanes): base state (modes 2, 3), then the accumulator;
             // mode 4 copies only the accumulator, to planes [0, nplanes)
             const int which = (a.mode == 4) ? 1 : (q >= nplanes);
             const int pl = q % nplanes;
-            const R *src = static_cast<const R *>(which ? a.acc : a.c) + pl * SE + static_cast<size_t>(tile) * kTile;
-            bulk_copy_g2s(s_pre + static_cast<size_t>(q) * kTile, src, bytes, bar);
+            const size_t g0 = pl * SE + static_cast<size_t>(tile) * kTile;
+            const size_t a0 = g0 & ~(A - 1), a1 = (g0 + cnt + A - 1) & ~(A - 1);
+            const R *src = static_cast<const R *>(which ? a.acc : a.c) + a0;
+            bulk_copy_g2s(s_pre + static_cast<size_t>(q) * a.prefetch, src, static_cast<unsigned>((a1 - a0) * sizeof(R)),
+                          bar);
         }
     }
 
@@ -351,6 +368,7 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
     R *__restrict__ out = static_cast<R *>(a.out);
     const R *pc = nullptr, *pacc = nullptr;   // base state / accumulator of this element
     size_t pstride = SE;
+    int sm = 0;   // prefetched: plane p's slice starts (p * sm) mod kPreAlign values into its copy
     if (pre) {
         if (!mbar_wait_bounded(bar, parity, 1ll << 26)) {
             // the copies did not land in time: report, wait once more for the
@@ -360,8 +378,9 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
             return pre;
         }
         pc = s_pre + row;
-        pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * kTile) + row;
-        pstride = kTile;
+        pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * a.prefetch) + row;
+        pstride = a.prefetch;
+        sm = static_cast<int>(SE & (kPreAlign - 1));
     } else {
         pc = static_cast<const R *>(a.c) + e;
         pacc = static_cast<const R *>(a.acc) + e;
@@ -396,7 +415,8 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
             for (int i = 0; i < NP; ++i) {
                 const R kk = sc * rhs[n][i];
                 const size_t o = ((V0 + n) * NP + i) * SE + e;
-                const size_t po = ((V0 + n) * NP + i) * pstride;
+                const int pi = (V0 + n) * NP + i;
+                const size_t po = pi * pstride + ((pi * sm) & (kPreAlign - 1));
                 out[o] = fma(alpha, kk, pc[po]);
                 acc[o] = fma(R(1.0 / 3.0), kk, pacc[po]);
             }
@@ -408,7 +428,8 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
                 const size_t o = ((V0 + n) * NP + i) * SE + e;
-                out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], pacc[((V0 + n) * NP + i) * pstride]);
+                const int pi = (V0 + n) * NP + i;
+                out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], pacc[pi * pstride + ((pi * sm) & (kPreAlign - 1))]);
             }
         break;
     }
@@ -705,7 +726,7 @@ template <int P, int EQ, bool BND>
 static int launch_one(const StageArgs &a_in, cudaStream_t st) {
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     StageArgs a = a_in;
-    if (a.prefetch && stage_smem_bytes<P, NV>(a.nslot, 1) > 200 * 1024) a.prefetch = 0;
+    if (a.prefetch && stage_smem_bytes<P, NV>(a.nslot, a.prefetch) > 200 * 1024) a.prefetch = 0;
     const size_t smem = stage_smem_bytes<P, NV>(a.nslot, a.prefetch);
     static size_t configured = 0;   // dynamic shared memory opted in so far
     if (smem > 48 * 1024 && smem > configured) {

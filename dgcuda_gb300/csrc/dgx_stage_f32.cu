@@ -13,8 +13,8 @@ int launch_batch_stage_f32_nb(int order, int equation, const BatchStageArgs &b, 
     return equation == DGX_EULER ? launch_batch_order<DGX_EULER>(order, b, st)
                                  : launch_batch_order<DGX_ADVECTION>(order, b, st);
 }
-size_t batch_smem_f32(int order, int equation, int nslot, int prefetch) {
-    return equation == DGX_EULER ? batch_smem_impl<DGX_EULER>(order, nslot, prefetch)
-                                 : batch_smem_impl<DGX_ADVECTION>(order, nslot, prefetch);
+size_t batch_smem_f32(int order, int equation, int nslot, int prefetch_plane) {
+    return equation == DGX_EULER ? batch_smem_impl<DGX_EULER>(order, nslot, prefetch_plane)
+                                 : batch_smem_impl<DGX_ADVECTION>(order, nslot, prefetch_plane);
 }
 }  // namespace dgx

@@ -58,7 +58,7 @@ template <int P, int NV>
 DGX_HD constexpr size_t tc_smem_bytes(int nslot, int prefetch) {
     return kSmemHead + tc_dims(P).bytes +
            sizeof(R) * (static_cast<size_t>(side_table_words<P, NV>()) + static_cast<size_t>(slot_words<P, NV>()) * nslot) +
-           (prefetch ? prefetch_bytes<P, NV>() : 0);
+           prefetch_bytes<P, NV>(prefetch);
 }
 
 constexpr unsigned kStatusMmaTimeout = kStatusCopyTimeout;
@@ -433,7 +433,7 @@ template <int P, int EQ, bool BND>
 int launch_tc_one(const StageArgs &a_in, cudaStream_t st) {
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     StageArgs a = a_in;
-    if (a.prefetch && tc_smem_bytes<P, NV>(a.nslot, 1) > 200 * 1024) a.prefetch = 0;
+    if (a.prefetch && tc_smem_bytes<P, NV>(a.nslot, a.prefetch) > 200 * 1024) a.prefetch = 0;
     const size_t smem = tc_smem_bytes<P, NV>(a.nslot, a.prefetch);
     if (smem > 227 * 1024) { set_error("tile halo too large for shared memory (%zu bytes)", smem); return DGX_ERR_UNSUPPORTED; }
     static size_t configured = 0;

@@ -258,15 +258,17 @@ def test_config2_vortex_reduced(gpu, oracle_mod):
     assert rel_l2(sv.get_state(), ref).max() <= FP32_TOL
 
 
-@pytest.mark.parametrize("n", [8, 5], ids=["aligned", "unaligned"])
-def test_prefetch_option_is_bitwise_neutral(n, gpu):
+@pytest.mark.parametrize("precision", [_ffi.FP32, _ffi.FP64, _ffi.FP32_BF16X3], ids=["fp32", "fp64", "bf16x3"])
+@pytest.mark.parametrize("n", [8, 5, 9, 13])
+def test_prefetch_option_is_bitwise_neutral(n, precision, gpu):
     """RK stages with the epilogue operands staged by the TMA engine give the
-    same bits as plain loads (E = 128: staged; E = 50: rows not 16-byte
-    aligned, so plain loads are used either way)."""
+    same bits as plain loads, whatever E (= 2 n^2: 128, 50, 162, 338) is
+    modulo the 16-byte alignment of the planes (the staged slices are widened
+    to 16-byte boundaries and read at their offset)."""
     m, eq, ic, params = make_case("vortex", 3, n=n, seed=4)
     out = []
     for pre in (1, 0):
-        sv = Solver(m, 3, eq, _ffi.FLUX_LLF, _ffi.FP32)
+        sv = Solver(m, 3, eq, _ffi.FLUX_LLF, precision)
         sv.set_option(_ffi.OPT_PREFETCH, pre)
         sv.project(ic, params)
         sv.set_dt(None)
