@@ -320,13 +320,14 @@ def run_batched(steps: int = 20):
             "tuned_options": opts, "unit": UNIT}
 
 
-def run_served(rates=(50, 200, 1000, 2000), count: int = 400):
+def run_served(rates=(50, 200, 1000, 2000, 0), count: int = 400):
     """Served configuration, scaled so every rate finishes in seconds: Poisson
     arrivals of `count` requests per rate, sizes N log-uniform in [16,64],
     orders 1..4, equations 50/50, end times U[0.1,1] x 0.02 flow-through times
     (the stated configuration's N up to 512 and full flow-through end times
     need hours per rate).  Also runs the same requests one by one on the plain
-    path for the throughput comparison."""
+    path for the throughput comparison.  Rate 0 submits every request at once:
+    the server's capacity, where the swept rates measure the offered load."""
     from dgcuda_gb300.serve import Server, request
     out = []
     rng = np.random.default_rng(12350)
@@ -338,7 +339,7 @@ def run_served(rates=(50, 200, 1000, 2000), count: int = 400):
             sp["t_end"] = flow * rng.uniform(0.1, 1.0) * 0.02
         srv = Server(budget_bytes=150 << 30, max_active=1024)
         srv.set_steps_per_check(4)
-        gaps = rng.exponential(1.0 / rate, size=count)
+        gaps = rng.exponential(1.0 / rate, size=count) if rate > 0 else np.zeros(count)
         t0 = time.perf_counter()
         t_next = t0
         for sp, g in zip(specs, gaps):
@@ -350,7 +351,7 @@ def run_served(rates=(50, 200, 1000, 2000), count: int = 400):
         wall = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
-        out.append({"rate_req_s": rate, "requests": count, "completed": st["completed"],
+        out.append({"rate_req_s": rate if rate > 0 else "all at once", "requests": count, "completed": st["completed"],
                     "failed": st["failed"], "p50_s": st["p50_latency_s"],
                     "p99_s": st["p99_latency_s"], "dof_updates": st["dof_updates"],
                     "value": st["dof_updates"] / wall, "wall_s": wall, "repacks": st["repacks"]})

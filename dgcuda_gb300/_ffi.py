@@ -55,7 +55,9 @@ class ServerStats(C.Structure):
                 ("steps", C.c_longlong), ("dof_updates", C.c_double),
                 ("busy_seconds", C.c_double), ("p50_latency_s", C.c_double),
                 ("p99_latency_s", C.c_double), ("max_latency_s", C.c_double),
-                ("device_bytes_in_use", C.c_size_t)]
+                ("device_bytes_in_use", C.c_size_t), ("admit_seconds", C.c_double),
+                ("repack_seconds", C.c_double), ("retire_seconds", C.c_double),
+                ("idle_seconds", C.c_double)]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = 0, 1, 2, 3, 4

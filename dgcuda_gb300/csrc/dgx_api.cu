@@ -82,11 +82,7 @@ int dalloc(T **p, size_t count, size_t *acct) {
 }
 
 void mesh_free(dgx_mesh *m) {
-    MeshDev &d = m->d;
-    void *ptrs[] = {d.V, d.elem_s, d.sides, d.J, d.xr, d.yr, d.xs, d.ys, d.diam, d.len, d.nx,
-                    d.ny, d.nbr, d.halo_off, d.halo_list, d.geo32, d.fn32, d.geo64, d.fn64};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    block_free(m->block);
     delete m;
 }
 
@@ -266,6 +262,192 @@ void set_error(const char *fmt, ...) {
     va_end(ap);
 }
 
+
+int mesh_build(int num_elem, int num_sides, const double *const Vs[6], const int *const es[3],
+               const int *const sd[4], BlockPool *pool, cudaStream_t st, const MeshBuildAsync *async,
+               dgx_mesh **out) {
+    if (!out) { set_error("out is NULL"); return DGX_ERR_INVALID; }
+    *out = nullptr;
+    if (num_elem <= 0 || num_sides <= 0 || num_elem > (1 << 28)) {
+        set_error("num_elem must be in 1..2^28 and num_sides >= 1");
+        return DGX_ERR_INVALID;
+    }
+    for (int i = 0; i < 6; ++i) if (!Vs[i]) { set_error("vertex array is NULL"); return DGX_ERR_INVALID; }
+    for (int i = 0; i < 3; ++i) if (!es[i]) { set_error("elem_s array is NULL"); return DGX_ERR_INVALID; }
+    for (int i = 0; i < 4; ++i) if (!sd[i]) { set_error("side array is NULL"); return DGX_ERR_INVALID; }
+    const double *V1x = Vs[0], *V1y = Vs[1], *V2x = Vs[2], *V2y = Vs[3], *V3x = Vs[4], *V3y = Vs[5];
+    const int *left_elem = sd[0], *right_elem = sd[1], *left_side_number = sd[2], *right_side_number = sd[3];
+    // host validation of the connectivity (the reference trusts its mesh file)
+    int nb = 0;
+    for (int s = 0; s < num_sides; ++s) {
+        const int L = left_elem[s], Rr = right_elem[s], ls = left_side_number[s], rs = right_side_number[s];
+        if (L < 0 || L >= num_elem || ls < 0 || ls > 2) { set_error("side %d: bad left element/side", s); return DGX_ERR_INVALID; }
+        if (es[ls][L] != s) { set_error("side %d: elem_s of its left element does not point back", s); return DGX_ERR_INVALID; }
+        if (Rr >= 0) {
+            if (Rr >= num_elem || rs < 0 || rs > 2) { set_error("side %d: bad right element/side", s); return DGX_ERR_INVALID; }
+            if (Rr == L) { set_error("side %d: left and right element coincide", s); return DGX_ERR_INVALID; }
+            if (es[rs][Rr] != s) { set_error("side %d: elem_s of its right element does not point back", s); return DGX_ERR_INVALID; }
+        } else {
+            if (Rr < -3) { set_error("side %d: boundary tag %d outside -3..-1", s, Rr); return DGX_ERR_INVALID; }
+            ++nb;
+        }
+    }
+    for (int e = 0; e < num_elem; ++e) {
+        for (int k = 0; k < 3; ++k)
+            if (es[k][e] < 0 || es[k][e] >= num_sides) { set_error("element %d: side index out of range", e); return DGX_ERR_INVALID; }
+        const double J = (V2x[e] - V1x[e]) * (V3y[e] - V1y[e]) - (V3x[e] - V1x[e]) * (V2y[e] - V1y[e]);
+        if (!(J > 0.0)) { set_error("element %d is not counter-clockwise (J = %g)", e, J); return DGX_ERR_INVALID; }
+    }
+
+    dgx_mesh *m = new (std::nothrow) dgx_mesh();
+    if (!m) { set_error("host allocation failed"); return DGX_ERR_NOMEM; }
+    cudaGetDevice(&m->device);
+    MeshDev &d = m->d;
+    d.num_elem = num_elem;
+    d.num_sides = num_sides;
+    d.num_boundary = nb;
+    const size_t E = num_elem, S = num_sides;
+    std::vector<int> words, hoff, hlist;
+    build_tiles(num_elem, es, left_elem, right_elem, left_side_number, right_side_number, words,
+                hoff, hlist, d.max_halo);
+    d.num_tiles = static_cast<int>(hoff.size()) - 1;
+    d.total_halo = static_cast<int>(hlist.size());
+    // one block: the arrays uploaded from the host first (one copy), then the
+    // ones the geometry kernels compute, then the reduction scratch
+    BlockLayout L;
+    const size_t oV = L.take<double>(6 * E), oEs = L.take<int>(3 * E), oSd = L.take<int>(4 * S),
+                 oNbr = L.take<int>(3 * E), oHoff = L.take<int>(hoff.size()), oHl = L.take<int>(hlist.size());
+    const size_t upload = L.size;
+    const size_t oJ = L.take<double>(E), oXr = L.take<double>(E), oYr = L.take<double>(E),
+                 oXs = L.take<double>(E), oYs = L.take<double>(E), oDiam = L.take<double>(E),
+                 oLen = L.take<double>(S), oNx = L.take<double>(S), oNy = L.take<double>(S),
+                 oG32 = L.take<float>(5 * E), oF32 = L.take<float>(9 * E), oG64 = L.take<double>(5 * E),
+                 oF64 = L.take<double>(9 * E);
+    // the minimum-diameter reduction: one partial per block of its fixed grid, then the result
+    const int red_len = static_cast<int>(std::min<size_t>((E + 255) / 256, kReduceLen));
+    const size_t oRed = L.take<double>(red_len + 1);
+    int rc = block_alloc(m->block, L.size, pool);
+    if (rc) { delete m; return rc; }
+    const DeviceBlock &b = m->block;
+    d.V = block_at<double>(b, oV); d.elem_s = block_at<int>(b, oEs); d.sides = block_at<int>(b, oSd);
+    d.nbr = block_at<int>(b, oNbr); d.halo_off = block_at<int>(b, oHoff); d.halo_list = block_at<int>(b, oHl);
+    d.J = block_at<double>(b, oJ); d.xr = block_at<double>(b, oXr); d.yr = block_at<double>(b, oYr);
+    d.xs = block_at<double>(b, oXs); d.ys = block_at<double>(b, oYs); d.diam = block_at<double>(b, oDiam);
+    d.len = block_at<double>(b, oLen); d.nx = block_at<double>(b, oNx); d.ny = block_at<double>(b, oNy);
+    d.geo32 = block_at<float>(b, oG32); d.fn32 = block_at<float>(b, oF32);
+    d.geo64 = block_at<double>(b, oG64); d.fn64 = block_at<double>(b, oF64);
+    std::vector<unsigned char> pageable;
+    unsigned char *stage = async && async->stage ? async->stage(upload) : nullptr;
+    if (!stage) {
+        pageable.assign(upload, 0);
+        stage = pageable.data();
+    }
+    auto put = [&](size_t off, const void *src, size_t bytes) {
+        if (bytes) std::memcpy(stage + off, src, bytes);
+    };
+    for (int i = 0; i < 6; ++i) put(oV + i * E * sizeof(double), Vs[i], E * sizeof(double));
+    for (int i = 0; i < 3; ++i) put(oEs + i * E * sizeof(int), es[i], E * sizeof(int));
+    for (int i = 0; i < 4; ++i) put(oSd + i * S * sizeof(int), sd[i], S * sizeof(int));
+    put(oNbr, words.data(), words.size() * sizeof(int));
+    put(oHoff, hoff.data(), hoff.size() * sizeof(int));
+    put(oHl, hlist.data(), hlist.size() * sizeof(int));
+    // from pageable memory the call returns once the bytes are staged, so
+    // `pageable` may go; pinned staging belongs to the caller
+    const cudaError_t ce = cudaMemcpyAsync(b.base, stage, upload, cudaMemcpyHostToDevice, st);
+    if (ce != cudaSuccess) { set_error("mesh upload failed: %s", cudaGetErrorString(ce)); mesh_free(m); return DGX_ERR_CUDA; }
+    rc = mesh_geometry(d, block_at<double>(b, oRed), red_len, async ? async->min_diam : nullptr, st);
+    if (!rc && !async && cudaStreamSynchronize(st) != cudaSuccess) { set_error("geometry kernels failed"); rc = DGX_ERR_CUDA; }
+    if (rc) {
+        if (async) cudaStreamSynchronize(st);   // queued work may still read the block
+        mesh_free(m);
+        return rc;
+    }
+    *out = m;
+    return DGX_OK;
+}
+
+int solver_build(dgx_mesh *mesh, const dgx_solver_desc *desc, BlockPool *pool, const double *scal_init,
+                 cudaStream_t st, dgx_solver **out) {
+    if (!mesh || !desc || !out) { set_error("NULL argument"); return DGX_ERR_INVALID; }
+    *out = nullptr;
+    if (desc->order < 0 || desc->order > kMaxOrder) { set_error("order %d outside 0..%d", desc->order, kMaxOrder); return DGX_ERR_UNSUPPORTED; }
+    if (desc->equation != DGX_ADVECTION && desc->equation != DGX_EULER) { set_error("unknown equation"); return DGX_ERR_INVALID; }
+    if (desc->flux != DGX_FLUX_CENTRAL && desc->flux != DGX_FLUX_LLF) { set_error("unknown flux"); return DGX_ERR_INVALID; }
+    if (desc->precision != DGX_FP32 && desc->precision != DGX_FP64 && desc->precision != DGX_FP32_BF16X3) {
+        set_error("unknown precision %d", desc->precision);
+        return DGX_ERR_INVALID;
+    }
+    if (desc->precision == DGX_FP32_BF16X3) {
+        if (desc->order < kTcMinOrder || desc->order > kTcMaxOrder) {
+            set_error("the BF16x3 path serves orders %d..%d", kTcMinOrder, kTcMaxOrder);
+            return DGX_ERR_UNSUPPORTED;
+        }
+        int rc = ensure_tensor_cores();
+        if (rc) return rc;
+    }
+    if (desc->integrator != DGX_RK4 && desc->integrator != DGX_RK2 && desc->integrator != DGX_FE) {
+        set_error("unknown integrator %d", desc->integrator);
+        return DGX_ERR_INVALID;
+    }
+    if (desc->equation == DGX_EULER && !(desc->gamma > 1.0)) { set_error("gamma must be > 1"); return DGX_ERR_INVALID; }
+    int rc = ensure_device_tables();
+    if (rc) return rc;
+    dgx_solver *sv = new (std::nothrow) dgx_solver();
+    if (!sv) { set_error("host allocation failed"); return DGX_ERR_NOMEM; }
+    SolverDev &s = sv->s;
+    s.order = desc->order;
+    s.np = num_modes(desc->order);
+    s.nv = desc->equation == DGX_EULER ? 4 : 1;
+    s.equation = desc->equation;
+    s.flux = desc->flux;
+    s.precision = desc->precision;
+    s.gamma = desc->gamma;
+    s.ax = desc->ax;
+    s.ay = desc->ay;
+    s.integrator = desc->integrator;
+    s.n = static_cast<size_t>(s.nv) * s.np * mesh->d.num_elem;
+    const size_t es = elem_size(s);
+    // one block: the device scalars (scal[8], lam_bits, counter, status, steps,
+    // chg_bits packed in 96 bytes), then c and ua for every integrator, and for
+    // RK4 its accumulator and a second stage input, each with 64 bytes of slack
+    // (the epilogue prefetch widens each slice to 16-byte boundaries)
+    constexpr size_t kHdr = 96;
+    BlockLayout L;
+    const size_t oHdr = L.take<unsigned char>(kHdr);
+    const int nbuf = s.integrator == DGX_RK4 ? 4 : 2;
+    size_t oBuf[4] = {0, 0, 0, 0};
+    for (int i = 0; i < nbuf; ++i) oBuf[i] = L.take<unsigned char>(s.n * es + 64);
+    rc = block_alloc(sv->block, L.size, pool);
+    if (rc) { delete sv; return rc; }
+    unsigned char *hdr = block_at<unsigned char>(sv->block, oHdr);
+    s.scal = reinterpret_cast<double *>(hdr);
+    s.lam_bits = reinterpret_cast<unsigned long long *>(hdr + 64);
+    s.counter = reinterpret_cast<unsigned int *>(hdr + 72);
+    s.status = reinterpret_cast<unsigned int *>(hdr + 76);
+    s.steps = reinterpret_cast<long long *>(hdr + 80);
+    s.chg_bits = reinterpret_cast<unsigned long long *>(hdr + 88);
+    void *bufs[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int i = 0; i < nbuf; ++i) bufs[i] = block_at<unsigned char>(sv->block, oBuf[i]);
+    s.c = bufs[0]; s.ua = bufs[1]; s.acc = bufs[2]; s.ub = bufs[3];
+    // the scalars by a kernel (its arguments are captured at launch): a copy
+    // from pageable memory would first wait for the stream
+    const double def[8] = {0.0, 0.0, 0.0, 0.0, 0.7, 0.0, 0.0, 0.0};
+    rc = init_solver_scalars(hdr, scal_init ? scal_init : def, st);
+    cudaError_t ce = rc ? cudaErrorLaunchFailure : cudaMemsetAsync(s.c, 0, s.n * es, st);
+    if (ce != cudaSuccess) {
+        set_error("solver init failed: %s", cudaGetErrorString(ce));
+        cudaStreamSynchronize(st);
+        block_free(sv->block);
+        delete sv;
+        return DGX_ERR_CUDA;
+    }
+    mesh->refs.fetch_add(1);
+    sv->mesh = mesh;
+    sv->device_bytes = L.size;
+    *out = sv;
+    return DGX_OK;
+}
+
 }  // namespace dgx
 
 using namespace dgx;
@@ -316,84 +498,10 @@ int dgx_mesh_create(int num_elem, int num_sides, const double *V1x, const double
                     const int *elem_s1, const int *elem_s2, const int *elem_s3,
                     const int *left_elem, const int *right_elem, const int *left_side_number,
                     const int *right_side_number, dgx_mesh **out) {
-    if (!out) { set_error("out is NULL"); return DGX_ERR_INVALID; }
-    *out = nullptr;
-    if (num_elem <= 0 || num_sides <= 0 || num_elem > (1 << 28)) {
-        set_error("num_elem must be in 1..2^28 and num_sides >= 1");
-        return DGX_ERR_INVALID;
-    }
     const double *Vs[6] = {V1x, V1y, V2x, V2y, V3x, V3y};
     const int *es[3] = {elem_s1, elem_s2, elem_s3};
     const int *sd[4] = {left_elem, right_elem, left_side_number, right_side_number};
-    for (auto p : Vs) if (!p) { set_error("vertex array is NULL"); return DGX_ERR_INVALID; }
-    for (auto p : es) if (!p) { set_error("elem_s array is NULL"); return DGX_ERR_INVALID; }
-    for (auto p : sd) if (!p) { set_error("side array is NULL"); return DGX_ERR_INVALID; }
-    // host validation of the connectivity (the reference trusts its mesh file)
-    int nb = 0;
-    for (int s = 0; s < num_sides; ++s) {
-        const int L = left_elem[s], Rr = right_elem[s], ls = left_side_number[s], rs = right_side_number[s];
-        if (L < 0 || L >= num_elem || ls < 0 || ls > 2) { set_error("side %d: bad left element/side", s); return DGX_ERR_INVALID; }
-        if (es[ls][L] != s) { set_error("side %d: elem_s of its left element does not point back", s); return DGX_ERR_INVALID; }
-        if (Rr >= 0) {
-            if (Rr >= num_elem || rs < 0 || rs > 2) { set_error("side %d: bad right element/side", s); return DGX_ERR_INVALID; }
-            if (Rr == L) { set_error("side %d: left and right element coincide", s); return DGX_ERR_INVALID; }
-            if (es[rs][Rr] != s) { set_error("side %d: elem_s of its right element does not point back", s); return DGX_ERR_INVALID; }
-        } else {
-            if (Rr < -3) { set_error("side %d: boundary tag %d outside -3..-1", s, Rr); return DGX_ERR_INVALID; }
-            ++nb;
-        }
-    }
-    for (int e = 0; e < num_elem; ++e) {
-        for (int k = 0; k < 3; ++k)
-            if (es[k][e] < 0 || es[k][e] >= num_sides) { set_error("element %d: side index out of range", e); return DGX_ERR_INVALID; }
-        const double J = (V2x[e] - V1x[e]) * (V3y[e] - V1y[e]) - (V3x[e] - V1x[e]) * (V2y[e] - V1y[e]);
-        if (!(J > 0.0)) { set_error("element %d is not counter-clockwise (J = %g)", e, J); return DGX_ERR_INVALID; }
-    }
-
-    dgx_mesh *m = new (std::nothrow) dgx_mesh();
-    if (!m) { set_error("host allocation failed"); return DGX_ERR_NOMEM; }
-    cudaGetDevice(&m->device);
-    MeshDev &d = m->d;
-    d.num_elem = num_elem;
-    d.num_sides = num_sides;
-    d.num_boundary = nb;
-    const size_t E = num_elem, S = num_sides;
-    int rc = DGX_OK;
-    size_t acct = 0;
-    rc |= dalloc(&d.V, 6 * E, &acct);
-    rc |= dalloc(&d.elem_s, 3 * E, &acct);
-    rc |= dalloc(&d.sides, 4 * S, &acct);
-    rc |= dalloc(&d.J, E, &acct); rc |= dalloc(&d.xr, E, &acct); rc |= dalloc(&d.yr, E, &acct);
-    rc |= dalloc(&d.xs, E, &acct); rc |= dalloc(&d.ys, E, &acct); rc |= dalloc(&d.diam, E, &acct);
-    rc |= dalloc(&d.len, S, &acct); rc |= dalloc(&d.nx, S, &acct); rc |= dalloc(&d.ny, S, &acct);
-    std::vector<int> words, hoff, hlist;
-    build_tiles(num_elem, es, left_elem, right_elem, left_side_number, right_side_number, words,
-                hoff, hlist, d.max_halo);
-    d.num_tiles = static_cast<int>(hoff.size()) - 1;
-    d.total_halo = static_cast<int>(hlist.size());
-    rc |= dalloc(&d.nbr, 3 * E, &acct);
-    rc |= dalloc(&d.halo_off, hoff.size(), &acct);
-    rc |= dalloc(&d.halo_list, hlist.size(), &acct);
-    rc |= dalloc(&d.geo32, 5 * E, &acct); rc |= dalloc(&d.fn32, 9 * E, &acct);
-    rc |= dalloc(&d.geo64, 5 * E, &acct); rc |= dalloc(&d.fn64, 9 * E, &acct);
-    if (rc) { mesh_free(m); return DGX_ERR_NOMEM; }
-    cudaError_t ce = cudaSuccess;
-    for (int i = 0; i < 6 && ce == cudaSuccess; ++i)
-        ce = cudaMemcpy(d.V + i * E, Vs[i], E * sizeof(double), cudaMemcpyHostToDevice);
-    for (int i = 0; i < 3 && ce == cudaSuccess; ++i)
-        ce = cudaMemcpy(d.elem_s + i * E, es[i], E * sizeof(int), cudaMemcpyHostToDevice);
-    for (int i = 0; i < 4 && ce == cudaSuccess; ++i)
-        ce = cudaMemcpy(d.sides + i * S, sd[i], S * sizeof(int), cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess) ce = cudaMemcpy(d.nbr, words.data(), words.size() * sizeof(int), cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess) ce = cudaMemcpy(d.halo_off, hoff.data(), hoff.size() * sizeof(int), cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess && !hlist.empty())
-        ce = cudaMemcpy(d.halo_list, hlist.data(), hlist.size() * sizeof(int), cudaMemcpyHostToDevice);
-    if (ce != cudaSuccess) { set_error("mesh upload failed: %s", cudaGetErrorString(ce)); mesh_free(m); return DGX_ERR_CUDA; }
-    rc = mesh_geometry(d, nullptr);
-    if (!rc && cudaDeviceSynchronize() != cudaSuccess) { set_error("geometry kernels failed"); rc = DGX_ERR_CUDA; }
-    if (rc) { mesh_free(m); return rc; }
-    *out = m;
-    return DGX_OK;
+    return mesh_build(num_elem, num_sides, Vs, es, sd, nullptr, nullptr, nullptr, out);
 }
 
 int dgx_mesh_destroy(dgx_mesh *mesh) {
@@ -430,86 +538,21 @@ int dgx_mesh_info(const dgx_mesh *mesh, int *num_elem, int *num_sides, int *num_
 }
 
 int dgx_solver_create(dgx_mesh *mesh, const dgx_solver_desc *desc, dgx_solver **out) {
-    if (!mesh || !desc || !out) { set_error("NULL argument"); return DGX_ERR_INVALID; }
-    *out = nullptr;
-    if (desc->order < 0 || desc->order > kMaxOrder) { set_error("order %d outside 0..%d", desc->order, kMaxOrder); return DGX_ERR_UNSUPPORTED; }
-    if (desc->equation != DGX_ADVECTION && desc->equation != DGX_EULER) { set_error("unknown equation"); return DGX_ERR_INVALID; }
-    if (desc->flux != DGX_FLUX_CENTRAL && desc->flux != DGX_FLUX_LLF) { set_error("unknown flux"); return DGX_ERR_INVALID; }
-    if (desc->precision != DGX_FP32 && desc->precision != DGX_FP64 && desc->precision != DGX_FP32_BF16X3) {
-        set_error("unknown precision %d", desc->precision);
-        return DGX_ERR_INVALID;
-    }
-    if (desc->precision == DGX_FP32_BF16X3) {
-        if (desc->order < kTcMinOrder || desc->order > kTcMaxOrder) {
-            set_error("the BF16x3 path serves orders %d..%d", kTcMinOrder, kTcMaxOrder);
-            return DGX_ERR_UNSUPPORTED;
-        }
-        int rc = ensure_tensor_cores();
-        if (rc) return rc;
-    }
-    if (desc->integrator != DGX_RK4 && desc->integrator != DGX_RK2 && desc->integrator != DGX_FE) {
-        set_error("unknown integrator %d", desc->integrator);
-        return DGX_ERR_INVALID;
-    }
-    if (desc->equation == DGX_EULER && !(desc->gamma > 1.0)) { set_error("gamma must be > 1"); return DGX_ERR_INVALID; }
-    int rc = ensure_device_tables();
+    int rc = solver_build(mesh, desc, nullptr, nullptr, nullptr, out);
     if (rc) return rc;
-    dgx_solver *sv = new (std::nothrow) dgx_solver();
-    if (!sv) { set_error("host allocation failed"); return DGX_ERR_NOMEM; }
-    SolverDev &s = sv->s;
-    s.order = desc->order;
-    s.np = num_modes(desc->order);
-    s.nv = desc->equation == DGX_EULER ? 4 : 1;
-    s.equation = desc->equation;
-    s.flux = desc->flux;
-    s.precision = desc->precision;
-    s.gamma = desc->gamma;
-    s.ax = desc->ax;
-    s.ay = desc->ay;
-    s.integrator = desc->integrator;
-    s.n = static_cast<size_t>(s.nv) * s.np * mesh->d.num_elem;
-    const size_t es = elem_size(s);
-    size_t acct = 0;
-    // c and ua for every integrator; RK4 adds its accumulator and a second stage input
-    char *bufs[4] = {nullptr, nullptr, nullptr, nullptr};
-    const int nbuf = s.integrator == DGX_RK4 ? 4 : 2;
-    // 64 bytes of slack: the epilogue prefetch widens each slice to 16-byte boundaries
-    for (int i = 0; i < nbuf && !rc; ++i) rc = dalloc(&bufs[i], s.n * es + 64, &acct);
-    if (!rc) rc = dalloc(&s.scal, 8, &acct);
-    if (!rc) rc = dalloc(&s.lam_bits, 1, &acct);
-    if (!rc) rc = dalloc(&s.counter, 1, &acct);
-    if (!rc) rc = dalloc(&s.status, 1, &acct);
-    if (!rc) rc = dalloc(&s.steps, 1, &acct);
-    if (!rc) rc = dalloc(&s.chg_bits, 1, &acct);
-    s.c = bufs[0]; s.ua = bufs[1]; s.acc = bufs[2]; s.ub = bufs[3];
-    if (!rc) {
-        const double init[8] = {0.0, 0.0, 0.0, 0.0, 0.7, 0.0, 0.0, 0.0};
-        cudaError_t ce = cudaMemcpy(s.scal, init, sizeof(init), cudaMemcpyHostToDevice);
-        if (ce == cudaSuccess) ce = cudaMemset(s.lam_bits, 0, sizeof(unsigned long long));
-        if (ce == cudaSuccess) ce = cudaMemset(s.counter, 0, sizeof(unsigned int));
-        if (ce == cudaSuccess) ce = cudaMemset(s.status, 0, sizeof(unsigned int));
-        if (ce == cudaSuccess) ce = cudaMemset(s.steps, 0, sizeof(long long));
-        if (ce == cudaSuccess) ce = cudaMemset(s.c, 0, s.n * es);
-        if (ce != cudaSuccess) { set_error("solver init failed: %s", cudaGetErrorString(ce)); rc = DGX_ERR_CUDA; }
+    if (cudaStreamSynchronize(nullptr) != cudaSuccess) {
+        set_error("solver initialisation failed: %s", cudaGetErrorString(cudaGetLastError()));
+        dgx_solver_destroy(*out);
+        *out = nullptr;
+        return DGX_ERR_CUDA;
     }
-    if (rc) {
-        sv->mesh = nullptr;
-        dgx_solver_destroy(sv);
-        return rc;
-    }
-    mesh->refs.fetch_add(1);
-    sv->mesh = mesh;
-    sv->device_bytes = acct;
-    *out = sv;
     return DGX_OK;
 }
 
 int dgx_solver_destroy(dgx_solver *sv) {
     if (!sv) return DGX_ERR_INVALID;
-    SolverDev &s = sv->s;
-    void *ptrs[] = {s.c, s.acc, s.ua, s.ub, s.scal, s.lam_bits, s.counter, s.status, s.steps, s.chg_bits, s.prev};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
+    block_free(sv->block);
+    if (sv->s.prev) cudaFree(sv->s.prev);
     if (sv->mesh) mesh_release(sv->mesh);
     delete sv;
     return DGX_OK;
@@ -584,6 +627,17 @@ int dgx_state_device_ptr(dgx_solver *sv, void **ptr) {
 }
 
 int dgx_project_ic(dgx_solver *sv, int ic, const double *params) {
+    const int rc = project_ic_on(sv, ic, params, nullptr);
+    if (rc) return rc;
+    DGX_TRY_CUDA(cudaDeviceSynchronize());
+    return DGX_OK;
+}
+
+}  // extern "C"
+
+namespace dgx {
+
+int project_ic_on(dgx_solver *sv, int ic, const double *params, cudaStream_t st) {
     if (!sv) return DGX_ERR_INVALID;
     if (ic < DGX_IC_GAUSSIAN || ic > DGX_IC_THREEPOINT) { set_error("unknown initial condition %d", ic); return DGX_ERR_INVALID; }
     if (sv->s.equation == DGX_EULER && (ic == DGX_IC_GAUSSIAN || ic == DGX_IC_POLY)) {
@@ -594,12 +648,15 @@ int dgx_project_ic(dgx_solver *sv, int ic, const double *params) {
         set_error("initial condition %d needs the Euler equations", ic);
         return DGX_ERR_INVALID;
     }
-    int rc = project_ic(sv->s, sv->mesh->d, ic, params, nullptr);
+    int rc = project_ic(sv->s, sv->mesh->d, ic, params, st);
     if (rc) return rc;
     sv->launches++;
-    DGX_TRY_CUDA(cudaDeviceSynchronize());
     return DGX_OK;
 }
+
+}  // namespace dgx
+
+extern "C" {
 
 int dgx_rhs_eval(dgx_solver *sv, const void *u, void *k, double dt, double t, void *stream) {
     if (!sv || !u || !k) return DGX_ERR_INVALID;

@@ -6,6 +6,10 @@
 #include <atomic>
 #include <cstddef>
 #include <cstdint>
+#include <functional>
+#include <map>
+#include <mutex>
+#include <vector>
 
 #include "dgx.h"
 #include "dgx_tables.h"
@@ -75,10 +79,69 @@ struct MeshDev {
     double *fn64 = nullptr;
 };
 
+// Device memory of meshes and solvers: every mesh and every solver keeps its
+// arrays in one block, carved at 256-byte boundaries.  A BlockPool keeps
+// released blocks by size class and hands them out again, so a long-running
+// owner (the request server) stops allocating and freeing device memory, and
+// with it the device-wide synchronisation of cudaFree, once its working set is
+// warm.  A block goes back to its pool only after the device work that reads
+// it has finished.
+class BlockPool {
+public:
+    static constexpr size_t kSlabBytes = static_cast<size_t>(64) << 20;
+    static constexpr size_t kSlabBlock = static_cast<size_t>(8) << 20;   // larger: one allocation each
+    explicit BlockPool(size_t keep_bytes) : keep_(keep_bytes) {}
+    ~BlockPool();   // frees the slabs: every block must have been returned
+    BlockPool(const BlockPool &) = delete;
+    BlockPool &operator=(const BlockPool &) = delete;
+    // a block of at least `bytes`; *got is its size (the size class)
+    int get(size_t bytes, void **p, size_t *got);
+    void put(void *p, size_t bytes);
+    void trim();                                   // free the cached blocks not carved from slabs
+    size_t cached_bytes();
+    long long hits() const { return hits_; }
+    long long misses() const { return misses_; }
+    // 4 KiB .. 64 KiB: powers of two; above: 8 classes per octave
+    static size_t size_class(size_t bytes);
+private:
+    std::mutex mu_;
+    std::multimap<size_t, void *> free_;
+    std::vector<void *> slabs_;
+    char *slab_next_ = nullptr;
+    size_t slab_left_ = 0;
+    size_t cached_ = 0, keep_;   // cached bytes of the blocks not carved from slabs
+    long long hits_ = 0, misses_ = 0;
+};
+
+struct DeviceBlock {
+    void *base = nullptr;
+    size_t bytes = 0;
+    BlockPool *pool = nullptr;   // nullptr: cudaMalloc / cudaFree
+};
+int block_alloc(DeviceBlock &b, size_t bytes, BlockPool *pool);
+void block_free(DeviceBlock &b);
+
+// offsets of consecutive arrays in one block, each at a 256-byte boundary
+struct BlockLayout {
+    size_t size = 0;
+    template <typename T>
+    size_t take(size_t count) {
+        size = (size + 255) & ~static_cast<size_t>(255);
+        const size_t at = size;
+        size += (count ? count : 1) * sizeof(T);
+        return at;
+    }
+};
+template <typename T>
+T *block_at(const DeviceBlock &b, size_t off) {
+    return reinterpret_cast<T *>(static_cast<char *>(b.base) + off);
+}
+
 }  // namespace dgx
 
 struct dgx_mesh {
     dgx::MeshDev d;
+    dgx::DeviceBlock block;
     int device = 0;
     std::atomic<int> refs{1};
 };
@@ -118,6 +181,7 @@ struct SolverDev {
 struct dgx_solver {
     dgx_mesh *mesh = nullptr;
     dgx::SolverDev s;
+    dgx::DeviceBlock block;
     size_t device_bytes = 0;
     long long launches = 0;
 };
@@ -225,8 +289,38 @@ int launch_batch_dt(const DtArgs *args, const int2 *items, int n_items, cudaStre
 StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c, void *acc,
                           void *out, double dt, double t);
 
+// Creation of meshes and solvers with their device memory from `pool`
+// (nullptr: cudaMalloc), uploads and initialisation on `st`.  Without `async`,
+// mesh_build returns once the geometry is computed.  With it nothing waits: the
+// upload goes through async->stage(bytes), pinned host memory that the caller
+// keeps until the stream has passed the copy (nullptr: a pageable copy), and the
+// minimum diameter lands in *async->min_diam (pinned) for the caller to store in
+// the mesh after synchronising the stream.  solver_build returns with its
+// initialisation queued on `st`; scal_init, when given, holds the 8 device
+// scalars (fixed dt, cfl, t_end ...).
+struct MeshBuildAsync {
+    std::function<unsigned char *(size_t)> stage;
+    double *min_diam = nullptr;
+};
+int mesh_build(int num_elem, int num_sides, const double *const Vs[6], const int *const es[3],
+               const int *const sd[4], BlockPool *pool, cudaStream_t st, const MeshBuildAsync *async,
+               dgx_mesh **out);
+int solver_build(dgx_mesh *mesh, const dgx_solver_desc *desc, BlockPool *pool, const double *scal_init,
+                 cudaStream_t st, dgx_solver **out);
+// dgx_project_ic without its closing synchronisation: validated, queued on st
+int project_ic_on(dgx_solver *sv, int ic, const double *params, cudaStream_t st);
+int periodic_square_arrays(int n, double lx, double ly, double x0, double y0, double jitter,
+                           unsigned long long seed, double *V, int *elem_s, int *sides);
+constexpr int kReduceLen = 4096;   // partial sums of the fixed-grid reductions
+
 // misc kernels (dgx_misc.cu)
-int mesh_geometry(MeshDev &m, cudaStream_t st);
+// geometry of an uploaded mesh; scratch holds scratch_len + 1 doubles, with
+// scratch_len = min(ceil(E / 256), kReduceLen) (the reduction's grid).  The
+// minimum diameter goes to m.min_diam (synchronous) or, with min_diam_dst (pinned
+// host memory), is copied there on st for the caller to collect after a sync.
+int mesh_geometry(MeshDev &m, double *scratch, int scratch_len, double *min_diam_dst, cudaStream_t st);
+// the 96-byte block of a solver's device scalars: scal[8] from scal8, the rest 0
+int init_solver_scalars(void *hdr, const double *scal8, cudaStream_t st);
 int project_ic(const SolverDev &s, const MeshDev &m, int ic, const double *params, cudaStream_t st);
 int launch_dt(SolverDev &s, const MeshDev &m, cudaStream_t st);
 // the p = 1 slope limiter on a state vector in place, and the largest
@@ -238,6 +332,11 @@ int commit_state(const SolverDev &s, void *dst, const void *src, cudaStream_t st
 // stages per step of an integrator
 inline int num_stages(int integrator) { return integrator == DGX_RK4 ? 4 : (integrator == DGX_RK2 ? 2 : 1); }
 int conserved_totals(SolverDev &s, const MeshDev &m, double *out, cudaStream_t st);
+// The same sums, queued on `st` without host synchronisation: terms holds E
+// doubles, scratch kReduceLen + 1; dev_sums[n] receives variable n's sum, to be
+// scaled by phi_0 / 2 on the host (bitwise the values conserved_totals returns).
+int conserved_sums_async(const SolverDev &s, const MeshDev &m, double *terms, double *scratch,
+                         double *dev_sums, cudaStream_t st);
 int convert_state(const void *src, int src_is_double, void *dst, int dst_is_double, size_t n,
                   cudaStream_t st);
 

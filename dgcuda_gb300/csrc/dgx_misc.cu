@@ -4,6 +4,8 @@
 #include <cmath>
 #include <vector>
 
+#include <cstring>
+
 #include "dgx_internal.h"
 #include "dgx_ic.cuh"
 
@@ -129,30 +131,47 @@ __global__ void mass_terms_kernel(const T *c, const double *J, int E, int np, in
 // ---------------------------------------------------------------------------
 struct IcArgs { double P[8]; };
 
+// L2 projection onto the modes: c_{n,i} = sum_q w_q U_n(x_q) phi_i(q) (the
+// basis is orthonormal with the reference triangle's area folded into w).  A
+// block takes kProjTile elements: its threads first evaluate the initial
+// condition at every (element, point) pair into shared memory, then sum every
+// (element, mode) pair over the points in order, so no per-thread accumulator
+// array spills and the transcendental work is done once per point.
+constexpr int kProjTile = 32;
+
 template <typename T>
-__global__ void project_kernel(MeshDev m, const Tables *tabs, int p, int nv, int ic, IcArgs A,
-                               double g, T *c) {
+__global__ void __launch_bounds__(kThreads) project_kernel(MeshDev m, const Tables *tabs, int p, int nv, int ic,
+                                                           IcArgs A, double g, T *c) {
+    __shared__ double sU[kMaxQuad * 4 * kProjTile];   // [q][n][element of the tile]
     const int E = m.num_elem;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= E) return;
+    const int e0 = blockIdx.x * kProjTile;
     const Tables &Tb = tabs[p];
+    const int nq = Tb.nq, np = Tb.np;
     const size_t SE = E;
-    const double v1x = m.V[e], v1y = m.V[SE + e], v2x = m.V[2 * SE + e], v2y = m.V[3 * SE + e];
-    const double v3x = m.V[4 * SE + e], v3y = m.V[5 * SE + e];
-    double acc[4][kMaxModes];
-    for (int n = 0; n < 4; ++n)
-        for (int i = 0; i < Tb.np; ++i) acc[n][i] = 0.0;
-    for (int q = 0; q < Tb.nq; ++q) {
+    for (int idx = threadIdx.x; idx < nq * kProjTile; idx += blockDim.x) {
+        const int q = idx / kProjTile, l = idx % kProjTile, e = e0 + l;
+        if (e >= E) continue;
+        const double v1x = m.V[e], v1y = m.V[SE + e], v2x = m.V[2 * SE + e], v2y = m.V[3 * SE + e];
+        const double v3x = m.V[4 * SE + e], v3y = m.V[5 * SE + e];
         const double r = Tb.r1[q], s = Tb.r2[q];
         const double x = r * v2x + s * v3x + (1 - r - s) * v1x;
         const double y = r * v2y + s * v3y + (1 - r - s) * v1y;
-        double U[4];
+        double U[4] = {0.0, 0.0, 0.0, 0.0};
         ic_eval(ic, A.P, g, x, y, U);
-        for (int i = 0; i < Tb.np; ++i)
-            for (int n = 0; n < nv; ++n) acc[n][i] += Tb.w[q] * U[n] * Tb.phi[i * Tb.nq + q];
+        for (int n = 0; n < 4; ++n) sU[(q * 4 + n) * kProjTile + l] = U[n];
     }
-    for (int n = 0; n < nv; ++n)
-        for (int i = 0; i < Tb.np; ++i) c[(static_cast<size_t>(n) * Tb.np + i) * SE + e] = static_cast<T>(acc[n][i]);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < np * kProjTile; idx += blockDim.x) {
+        const int i = idx / kProjTile, l = idx % kProjTile, e = e0 + l;
+        if (e >= E) continue;
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int q = 0; q < nq; ++q) {
+            const double wq = Tb.w[q], ph = Tb.phi[i * nq + q];
+#pragma unroll
+            for (int n = 0; n < 4; ++n) acc[n] += wq * sU[(q * 4 + n) * kProjTile + l] * ph;
+        }
+        for (int n = 0; n < nv; ++n) c[(static_cast<size_t>(n) * np + i) * SE + e] = static_cast<T>(acc[n]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -257,18 +276,27 @@ __global__ void convert_kernel(const void *src, int src_double, T *dst, size_t n
 
 int blocks_for(size_t n) { return static_cast<int>((n + kThreads - 1) / kThreads); }
 
-// deterministic reduction of x[0..n) with a fixed grid; result to *host
-int reduce_host(const double *x, size_t n, int op, double *scratch, int scratch_len, double *host,
-                cudaStream_t st) {
+// deterministic reduction of x[0..n) with a fixed grid (scratch_len partials);
+// the result to the device double *result
+int reduce_dev(const double *x, size_t n, int op, double *scratch, int scratch_len, double *result,
+               cudaStream_t st) {
     int grid = static_cast<int>((n + kThreads - 1) / kThreads);
     if (grid > scratch_len) grid = scratch_len;
     if (grid < 1) grid = 1;
     if (op == 0) reduce_kernel<0><<<grid, kThreads, 0, st>>>(x, n, scratch, 0.0);
     else reduce_kernel<1><<<grid, kThreads, 0, st>>>(x, n, scratch, INFINITY);
     DGX_CHECK_LAUNCH();
-    if (op == 0) reduce_kernel<0><<<1, kThreads, 0, st>>>(scratch, grid, scratch + scratch_len, 0.0);
-    else reduce_kernel<1><<<1, kThreads, 0, st>>>(scratch, grid, scratch + scratch_len, INFINITY);
+    if (op == 0) reduce_kernel<0><<<1, kThreads, 0, st>>>(scratch, grid, result, 0.0);
+    else reduce_kernel<1><<<1, kThreads, 0, st>>>(scratch, grid, result, INFINITY);
     DGX_CHECK_LAUNCH();
+    return DGX_OK;
+}
+
+// the same, result to *host (synchronous)
+int reduce_host(const double *x, size_t n, int op, double *scratch, int scratch_len, double *host,
+                cudaStream_t st) {
+    const int rc = reduce_dev(x, n, op, scratch, scratch_len, scratch + scratch_len, st);
+    if (rc) return rc;
     DGX_TRY_CUDA(cudaMemcpyAsync(host, scratch + scratch_len, sizeof(double), cudaMemcpyDeviceToHost, st));
     DGX_TRY_CUDA(cudaStreamSynchronize(st));
     return DGX_OK;
@@ -281,7 +309,7 @@ int upload_tables_misc() {
     return dev_tables(&t);
 }
 
-int mesh_geometry(MeshDev &m, cudaStream_t st) {
+int mesh_geometry(MeshDev &m, double *scratch, int scratch_len, double *min_diam_dst, cudaStream_t st) {
     const int E = m.num_elem, S = m.num_sides;
     elem_geometry_kernel<<<blocks_for(E), kThreads, 0, st>>>(m);
     DGX_CHECK_LAUNCH();
@@ -290,12 +318,11 @@ int mesh_geometry(MeshDev &m, cudaStream_t st) {
     elem_side_kernel<<<blocks_for(E), kThreads, 0, st>>>(m);
     DGX_CHECK_LAUNCH();
     // minimum inscribed diameter (exact: min is order independent)
-    const int len = 4096;
-    double *scratch = nullptr;
-    DGX_TRY_CUDA(cudaMalloc(&scratch, sizeof(double) * (len + 1)));
-    int rc = reduce_host(m.diam, E, 1, scratch, len, &m.min_diam, st);
-    cudaFree(scratch);
-    return rc;
+    if (!min_diam_dst) return reduce_host(m.diam, E, 1, scratch, scratch_len, &m.min_diam, st);
+    const int rc = reduce_dev(m.diam, E, 1, scratch, scratch_len, scratch + scratch_len, st);
+    if (rc) return rc;
+    DGX_TRY_CUDA(cudaMemcpyAsync(min_diam_dst, scratch + scratch_len, sizeof(double), cudaMemcpyDeviceToHost, st));
+    return DGX_OK;
 }
 
 int project_ic(const SolverDev &s, const MeshDev &m, int ic, const double *params, cudaStream_t st) {
@@ -304,12 +331,13 @@ int project_ic(const SolverDev &s, const MeshDev &m, int ic, const double *param
     if (rc) return rc;
     IcArgs A;
     for (int i = 0; i < 8; ++i) A.P[i] = params ? params[i] : 0.0;
+    const int grid = (m.num_elem + kProjTile - 1) / kProjTile;
     if (s.precision == DGX_FP64)
-        project_kernel<double><<<blocks_for(m.num_elem), kThreads, 0, st>>>(
-            m, tabs, s.order, s.nv, ic, A, s.gamma, static_cast<double *>(s.c));
+        project_kernel<double><<<grid, kThreads, 0, st>>>(m, tabs, s.order, s.nv, ic, A, s.gamma,
+                                                          static_cast<double *>(s.c));
     else
-        project_kernel<float><<<blocks_for(m.num_elem), kThreads, 0, st>>>(
-            m, tabs, s.order, s.nv, ic, A, s.gamma, static_cast<float *>(s.c));
+        project_kernel<float><<<grid, kThreads, 0, st>>>(m, tabs, s.order, s.nv, ic, A, s.gamma,
+                                                         static_cast<float *>(s.c));
     DGX_CHECK_LAUNCH();
     return DGX_OK;
 }
@@ -358,7 +386,7 @@ int launch_batch_dt(const DtArgs *args, const int2 *items, int n_items, cudaStre
 int conserved_totals(SolverDev &s, const MeshDev &m, double *out, cudaStream_t st) {
     const int E = m.num_elem;
     double *terms = nullptr;
-    const int len = 4096;
+    const int len = kReduceLen;
     double *scratch = nullptr;
     DGX_TRY_CUDA(cudaMalloc(&terms, sizeof(double) * E));
     if (cudaMalloc(&scratch, sizeof(double) * (len + 1)) != cudaSuccess) {
@@ -383,6 +411,38 @@ int conserved_totals(SolverDev &s, const MeshDev &m, double *out, cudaStream_t s
     cudaFree(terms);
     cudaFree(scratch);
     return rc;
+}
+
+namespace {
+struct Words12 { unsigned long long w[12]; };
+__global__ void init_words_kernel(unsigned long long *dst, Words12 v) {
+    if (threadIdx.x < 12) dst[threadIdx.x] = v.w[threadIdx.x];
+}
+}  // namespace
+
+int init_solver_scalars(void *hdr, const double *scal8, cudaStream_t st) {
+    Words12 v{};
+    std::memcpy(v.w, scal8, 8 * sizeof(double));
+    init_words_kernel<<<1, 32, 0, st>>>(static_cast<unsigned long long *>(hdr), v);
+    DGX_CHECK_LAUNCH();
+    return DGX_OK;
+}
+
+int conserved_sums_async(const SolverDev &s, const MeshDev &m, double *terms, double *scratch,
+                         double *dev_sums, cudaStream_t st) {
+    const int E = m.num_elem;
+    for (int n = 0; n < s.nv; ++n) {
+        if (s.precision == DGX_FP64)
+            mass_terms_kernel<double><<<blocks_for(E), kThreads, 0, st>>>(
+                static_cast<const double *>(s.c), m.J, E, s.np, n, terms);
+        else
+            mass_terms_kernel<float><<<blocks_for(E), kThreads, 0, st>>>(
+                static_cast<const float *>(s.c), m.J, E, s.np, n, terms);
+        DGX_CHECK_LAUNCH();
+        const int rc = reduce_dev(terms, E, 0, scratch, kReduceLen, dev_sums + n, st);
+        if (rc) return rc;
+    }
+    return DGX_OK;
 }
 
 int convert_state(const void *src, int src_is_double, void *dst, int dst_is_double, size_t n,

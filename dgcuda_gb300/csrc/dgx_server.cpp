@@ -20,6 +20,7 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <set>
 #include <thread>
 #include <tuple>
 #include <vector>
@@ -51,12 +52,19 @@ struct Request {
 
 using MeshKey = std::tuple<int, double, double, double, unsigned long long>;
 
-size_t estimate_bytes(const dgx_request &r, bool mesh_cached) {
+// device footprint of a request's mesh and solver blocks (their size classes)
+size_t mesh_estimate(const dgx_request &r) {
     const size_t E = 2 * static_cast<size_t>(r.n) * r.n, S = 3 * static_cast<size_t>(r.n) * r.n;
+    const size_t red = std::min<size_t>((E + 255) / 256, kReduceLen) + 1;
+    const size_t mesh = E * (6 * 8 + 3 * 4 + 6 * 8 + 3 * 4 + 5 * 4 + 9 * 4 + 5 * 8 + 9 * 8 + 4) +
+                        S * (4 * 4 + 3 * 8) + red * 8 + 20 * 256;
+    return BlockPool::size_class(mesh);
+}
+size_t solver_estimate(const dgx_request &r) {
+    const size_t E = 2 * static_cast<size_t>(r.n) * r.n;
     const size_t np = static_cast<size_t>(num_modes(r.order)), nv = r.equation == DGX_EULER ? 4 : 1;
     const size_t vb = r.precision == DGX_FP64 ? 8 : 4;
-    size_t mesh = E * (6 * 8 + 3 * 4 + 6 * 8 + 3 * 4 + 5 * 4 + 9 * 4 + 5 * 8 + 9 * 8 + 4) + S * (4 * 4 + 3 * 8);
-    return (mesh_cached ? 0 : mesh) + 4 * nv * np * E * vb + 4096;
+    return BlockPool::size_class(4 * (nv * np * E * vb + 64 + 256) + 256);
 }
 
 }  // namespace
@@ -74,10 +82,30 @@ struct dgx_server {
     std::map<long long, Request *> all;
     std::vector<Request *> active;
     int in_transit = 0;   // admitted, out of the queue, not yet active or finished
-    std::map<MeshKey, dgx_mesh *> meshes;     // shared meshes (refcounted by their solvers)
+    // shared meshes, refcounted by their solvers; meshes no running solve uses
+    // stay cached (least recently used first out) while the budget allows
+    struct CachedMesh {
+        dgx_mesh *mesh = nullptr;
+        size_t bytes = 0;
+        long long last_use = 0;
+    };
+    std::map<MeshKey, CachedMesh> meshes;
+    size_t mesh_bytes = 0;   // footprint of the cached meshes, counted against the budget
+    long long use_tick = 0;
+    dgx::BlockPool *pool = nullptr;   // mesh and solver blocks, recycled
+    double *red = nullptr;            // conserved-total scratch: terms, partials, sums
+    size_t red_elems = 0, red_solves = 0;
+    std::vector<double> sums;
+    // pinned host memory of an admission round: mesh uploads (bump-allocated,
+    // reused once the stream has passed them) and the meshes' minimum diameters
+    unsigned char *stage = nullptr;
+    size_t stage_cap = 0, stage_off = 0;
+    double *min_diam = nullptr;
+    size_t min_diam_cap = 0;
     std::vector<double> latencies;
     long long next_id = 1, submitted = 0, completed = 0, failed = 0, repacks = 0, steps = 0;
     double dof_updates = 0.0, busy = 0.0;
+    double admit_s = 0.0, repack_s = 0.0, retire_s = 0.0, idle_s = 0.0;   // worker time by phase
     bool stop = false;
     std::thread worker;
     dgx_batch *batch = nullptr;
@@ -100,13 +128,112 @@ int validate(const dgx_request &r) {
 }
 
 void release_solve(dgx_server *s, Request *q) {
-    if (q->solver) dgx_solver_destroy(q->solver);
+    if (q->solver) dgx_solver_destroy(q->solver);   // its blocks go back to the pool
     q->solver = nullptr;
     q->mesh = nullptr;   // owned by the mesh cache
     s->in_use -= std::min(s->in_use, q->bytes);
 }
 
-// create the solver of a request (worker thread, lock not held)
+MeshKey mesh_key(const dgx_request &r) { return MeshKey{r.n, r.lx, r.ly, r.jitter, r.seed}; }
+
+// Drop cached meshes that no running solve uses, least recently used first,
+// until `free_target` bytes of the budget are free or only `keep_idle` idle
+// meshes remain (lock held; keys in `pinned` are about to be used).
+void evict_idle_meshes(dgx_server *s, size_t free_target, size_t keep_idle, const std::set<MeshKey> &pinned) {
+    std::vector<std::pair<long long, MeshKey>> idle;
+    for (auto &kv : s->meshes)
+        if (kv.second.mesh && kv.second.mesh->refs.load() == 1 && !pinned.count(kv.first))
+            idle.emplace_back(kv.second.last_use, kv.first);
+    std::sort(idle.begin(), idle.end());
+    size_t left = idle.size();
+    for (auto &it : idle) {
+        const bool room = s->in_use + s->mesh_bytes + free_target <= s->budget;
+        if (room && left <= keep_idle) break;
+        auto m = s->meshes.find(it.second);
+        s->mesh_bytes -= std::min(s->mesh_bytes, m->second.bytes);
+        dgx_mesh_destroy(m->second.mesh);
+        s->meshes.erase(m);
+        --left;
+    }
+}
+
+// pinned staging for one mesh upload of the current admission round
+unsigned char *stage_bytes(dgx_server *s, size_t bytes) {
+    bytes = (bytes + 255) & ~static_cast<size_t>(255);
+    if (s->stage_off + bytes > s->stage_cap) {
+        if (cudaStreamSynchronize(s->stream) != cudaSuccess) return nullptr;   // the arena's copies are done
+        s->stage_off = 0;
+        if (bytes > s->stage_cap) {
+            if (s->stage) cudaFreeHost(s->stage);
+            s->stage = nullptr;
+            s->stage_cap = 0;
+            const size_t cap = std::max(bytes, static_cast<size_t>(16) << 20);
+            if (cudaMallocHost(&s->stage, cap) != cudaSuccess) {
+                cudaGetLastError();
+                s->stage = nullptr;
+                return nullptr;   // the build falls back to a pageable copy
+            }
+            s->stage_cap = cap;
+        }
+    }
+    unsigned char *p = s->stage + s->stage_off;
+    s->stage_off += bytes;
+    return p;
+}
+
+// the request's mesh, from the cache or built (worker thread, lock not held;
+// the cache entry and its bytes were reserved at admission).  A mesh built here
+// gets its minimum diameter at the round's synchronisation: its slot is
+// appended to `fresh`.
+dgx_mesh *cached_mesh(dgx_server *s, const dgx_request &r, int *rc,
+                      std::vector<std::pair<dgx_mesh *, size_t>> &fresh) {
+    const MeshKey key = mesh_key(r);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->meshes.find(key);
+        if (it != s->meshes.end() && it->second.mesh) {
+            it->second.last_use = ++s->use_tick;
+            return it->second.mesh;
+        }
+    }
+    const size_t E = 2 * static_cast<size_t>(r.n) * r.n, S = 3 * static_cast<size_t>(r.n) * r.n;
+    std::vector<double> V(6 * E);
+    std::vector<int> es(3 * E), sd(4 * S);
+    dgx_mesh *m = nullptr;
+    *rc = periodic_square_arrays(r.n, r.lx, r.ly, 0.0, 0.0, r.jitter, r.seed, V.data(), es.data(), sd.data());
+    if (!*rc) {
+        const double *Vs[6] = {V.data(), V.data() + E, V.data() + 2 * E, V.data() + 3 * E, V.data() + 4 * E, V.data() + 5 * E};
+        const int *ep[3] = {es.data(), es.data() + E, es.data() + 2 * E};
+        const int *sp[4] = {sd.data(), sd.data() + S, sd.data() + 2 * S, sd.data() + 3 * S};
+        MeshBuildAsync as;
+        as.stage = [s](size_t bytes) { return stage_bytes(s, bytes); };
+        as.min_diam = fresh.size() < s->min_diam_cap ? s->min_diam + fresh.size() : nullptr;
+        *rc = mesh_build(static_cast<int>(E), static_cast<int>(S), Vs, ep, sp, s->pool, s->stream,
+                         as.min_diam ? &as : nullptr, &m);
+        if (!*rc && as.min_diam) fresh.emplace_back(m, fresh.size());
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->meshes.find(key);
+    if (*rc) {
+        if (it != s->meshes.end() && !it->second.mesh) {   // give the reservation back
+            s->mesh_bytes -= std::min(s->mesh_bytes, it->second.bytes);
+            s->meshes.erase(it);
+        }
+        return nullptr;
+    }
+    if (it == s->meshes.end()) {
+        it = s->meshes.emplace(key, dgx_server::CachedMesh{}).first;
+        it->second.bytes = mesh_estimate(r);
+        s->mesh_bytes += it->second.bytes;
+    }
+    it->second.mesh = m;
+    it->second.last_use = ++s->use_tick;
+    return m;
+}
+
+// create the solver of a request (worker thread, lock not held): block from the
+// pool, initial scalars (dt rule, cfl, end time) and the projected initial
+// condition queued on the server's stream, no host synchronisation
 int start_solve(dgx_server *s, Request *q, dgx_mesh *mesh) {
     dgx_solver_desc d;
     d.order = q->r.order;
@@ -117,29 +244,60 @@ int start_solve(dgx_server *s, Request *q, dgx_mesh *mesh) {
     d.gamma = q->r.gamma;
     d.ax = q->r.ax;
     d.ay = q->r.ay;
-    int rc = dgx_solver_create(mesh, &d, &q->solver);
-    if (!rc) rc = dgx_project_ic(q->solver, q->r.ic, q->r.params);
-    if (!rc) rc = q->r.dt > 0.0 ? dgx_set_dt(q->solver, DGX_DT_FIXED, q->r.dt, 0.7)
-                                : dgx_set_dt(q->solver, DGX_DT_CFL, 0.0, q->r.cfl);
-    if (!rc) rc = dgx_set_end_time(q->solver, q->r.t_end);
+    const bool fixed = q->r.dt > 0.0;
+    // device scalars: [3] fixed dt, [4] cfl, [5] t_end (the values dgx_set_dt and
+    // dgx_set_end_time write)
+    const double scal[8] = {0.0, 0.0, 0.0, fixed ? q->r.dt : 0.0, fixed ? 0.7 : q->r.cfl, q->r.t_end, 0.0, 0.0};
+    int rc = solver_build(mesh, &d, s->pool, scal, s->stream, &q->solver);
+    if (!rc) {
+        q->solver->s.dt_mode = fixed ? DGX_DT_FIXED : DGX_DT_CFL;
+        rc = project_ic_on(q->solver, q->r.ic, q->r.params, s->stream);
+    }
     if (!rc) {
         int nv = 0, np = 0;
         dgx_solver_info(q->solver, &nv, &np, nullptr, nullptr);
         q->dofs = static_cast<long long>(nv) * np * 2LL * q->r.n * q->r.n;
     }
-    (void)s;
     return rc;
 }
 
-dgx_mesh *cached_mesh(dgx_server *s, const dgx_request &r, int *rc) {
-    const MeshKey key{r.n, r.lx, r.ly, r.jitter, r.seed};
-    auto it = s->meshes.find(key);
-    if (it != s->meshes.end()) return it->second;
-    dgx_mesh *m = nullptr;
-    *rc = dgx_mesh_create_periodic_square(r.n, r.lx, r.ly, 0.0, 0.0, r.jitter, r.seed, &m);
-    if (*rc) return nullptr;
-    s->meshes[key] = m;
-    return m;
+// Conserved totals of finished solves: all their reductions queued on the
+// server's stream, one copy back (the same kernels, grid and order as
+// dgx_conserved_totals, so the same bits).
+int retire_totals(dgx_server *s, const std::vector<Request *> &done) {
+    if (done.empty()) return DGX_OK;
+    size_t emax = 0;
+    for (Request *q : done) emax = std::max(emax, static_cast<size_t>(q->solver->mesh->d.num_elem));
+    if (emax > s->red_elems || done.size() > s->red_solves) {
+        if (s->red) cudaFree(s->red);   // the stream is idle here
+        s->red = nullptr;
+        s->red_elems = std::max(emax, s->red_elems);
+        s->red_solves = std::max(done.size(), s->red_solves);
+        const size_t n = s->red_elems + kReduceLen + 1 + 4 * s->red_solves;
+        if (cudaMalloc(&s->red, n * sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            s->red = nullptr;
+            s->red_elems = s->red_solves = 0;
+            set_error("conserved-total scratch allocation failed");
+            return DGX_ERR_NOMEM;
+        }
+    }
+    double *terms = s->red, *partials = s->red + s->red_elems, *sums = partials + kReduceLen + 1;
+    for (size_t j = 0; j < done.size(); ++j) {
+        const dgx_solver *sv = done[j]->solver;
+        int rc = conserved_sums_async(sv->s, sv->mesh->d, terms, partials, sums + 4 * j, s->stream);
+        if (rc) return rc;
+    }
+    s->sums.resize(4 * done.size());
+    DGX_TRY_CUDA(cudaMemcpyAsync(s->sums.data(), sums, sizeof(double) * 4 * done.size(), cudaMemcpyDeviceToHost,
+                                 s->stream));
+    DGX_TRY_CUDA(cudaStreamSynchronize(s->stream));
+    for (size_t j = 0; j < done.size(); ++j) {
+        Request *q = done[j];
+        const double phi0 = tables(q->solver->s.order).phi[0];
+        for (int n = 0; n < q->solver->s.nv; ++n) q->totals[n] = s->sums[4 * j + n] * phi0 * 0.5;
+    }
+    return DGX_OK;
 }
 
 void finish(dgx_server *s, Request *q, int state, int status) {
@@ -154,6 +312,8 @@ void finish(dgx_server *s, Request *q, int state, int status) {
     }
 }
 
+constexpr size_t kIdleMeshes = 32;   // idle meshes kept for requests that share them
+
 void worker_main(dgx_server *s) {
     cudaSetDevice(s->device);
     cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
@@ -167,10 +327,13 @@ void worker_main(dgx_server *s) {
             std::unique_lock<std::mutex> lk(s->mu);
             if (s->active.empty() && s->queue.empty() && !s->stop) {
                 s->idle_cv.notify_all();
+                const auto tw = Clock::now();
                 s->cv.wait(lk, [&] { return s->stop || !s->queue.empty(); });
+                s->idle_s += std::chrono::duration<double>(Clock::now() - tw).count();
             }
             if (s->stop) break;
             // admission by device-memory footprint and slot count, in arrival order
+            std::set<MeshKey> pinned;
             while (!s->queue.empty() && static_cast<int>(s->active.size() + admit.size()) < s->max_active) {
                 Request *q = s->queue.front();
                 if (q->cancel) {
@@ -178,31 +341,69 @@ void worker_main(dgx_server *s) {
                     q->state = kCancelled;
                     continue;
                 }
-                const MeshKey key{q->r.n, q->r.lx, q->r.ly, q->r.jitter, q->r.seed};
-                const size_t need = estimate_bytes(q->r, s->meshes.count(key) > 0);
-                if (s->in_use + need > s->budget && !(s->active.empty() && admit.empty())) break;
+                const MeshKey key = mesh_key(q->r);
+                const bool cached = s->meshes.count(key) > 0;
+                const size_t need = solver_estimate(q->r) + (cached ? 0 : mesh_estimate(q->r));
+                pinned.insert(key);
+                if (s->in_use + s->mesh_bytes + need > s->budget) evict_idle_meshes(s, need, 0, pinned);
+                if (s->in_use + s->mesh_bytes + need > s->budget && !(s->active.empty() && admit.empty())) break;
                 s->queue.pop_front();
-                q->bytes = need;
-                s->in_use += need;
+                if (!cached) {   // reserve the mesh's bytes until it is built
+                    auto &cm = s->meshes[key];
+                    cm.bytes = mesh_estimate(q->r);
+                    s->mesh_bytes += cm.bytes;
+                }
+                q->bytes = solver_estimate(q->r);
+                s->in_use += q->bytes;
                 admit.push_back(q);
                 s->in_transit++;
             }
         }
+        const auto ta = Clock::now();
+        std::vector<Request *> started;
+        std::vector<std::pair<dgx_mesh *, size_t>> fresh;
+        s->stage_off = 0;   // the stream is idle between rounds
+        if (admit.size() > s->min_diam_cap) {
+            if (s->min_diam) cudaFreeHost(s->min_diam);
+            s->min_diam = nullptr;
+            s->min_diam_cap = 0;
+            const size_t cap = std::max(admit.size(), static_cast<size_t>(256));
+            if (cudaMallocHost(&s->min_diam, cap * sizeof(double)) == cudaSuccess) s->min_diam_cap = cap;
+            else cudaGetLastError();   // meshes are then built synchronously
+        }
         for (Request *q : admit) {
             int rc = DGX_OK;
-            dgx_mesh *m = cached_mesh(s, q->r, &rc);   // the cache is the worker's alone
+            dgx_mesh *m = cached_mesh(s, q->r, &rc, fresh);
             if (!rc) rc = start_solve(s, q, m);
+            if (!rc) { started.push_back(q); continue; }
             std::lock_guard<std::mutex> lk(s->mu);
             s->in_transit--;
-            if (rc) {
-                release_solve(s, q);
-                finish(s, q, kFailed, rc);
-            } else {
+            release_solve(s, q);
+            finish(s, q, kFailed, rc);
+        }
+        if (!started.empty() || !fresh.empty()) {
+            // one synchronisation for the whole admission round: the uploads and
+            // projections have run (and any fault of theirs shows here)
+            const cudaError_t ce = cudaStreamSynchronize(s->stream);
+            for (auto &f : fresh) f.first->d.min_diam = s->min_diam[f.second];
+            std::lock_guard<std::mutex> lk(s->mu);
+            for (Request *q : started) {
+                s->in_transit--;
+                if (ce != cudaSuccess) {
+                    release_solve(s, q);
+                    finish(s, q, kFailed, DGX_ERR_CUDA);
+                    continue;
+                }
                 q->state = kRunning;
                 q->started = Clock::now();
                 s->active.push_back(q);
                 changed = true;
             }
+        }
+        const auto tr = Clock::now();
+        if (!admit.empty()) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->admit_s += std::chrono::duration<double>(tr - ta).count();
         }
         if (s->active.empty()) continue;
         // repack the active set into one batch
@@ -221,6 +422,10 @@ void worker_main(dgx_server *s) {
             }
         }
         const auto t0 = Clock::now();
+        if (t0 > tr) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->repack_s += std::chrono::duration<double>(t0 - tr).count();
+        }
         dgx_batch_run(s->batch, s->steps_per_check, s->stream);
         const size_t n = s->active.size();
         t.resize(n); dt.resize(n); st.resize(n); stp.resize(n);
@@ -228,7 +433,9 @@ void worker_main(dgx_server *s) {
         if (s->stall_seconds > 0.0)   // host-side fault injection: a stalled worker
             std::this_thread::sleep_for(std::chrono::duration<double>(s->stall_seconds));
         const auto t1 = Clock::now();
-        std::vector<Request *> keep;
+        // finished solves: totals (and kept states) read back, then released
+        std::vector<Request *> keep, done, leaving;
+        std::vector<double> t_done;
         {
             std::lock_guard<std::mutex> lk(s->mu);
             s->busy += std::chrono::duration<double>(t1 - t0).count();
@@ -239,36 +446,63 @@ void worker_main(dgx_server *s) {
                 s->dof_updates += static_cast<double>(done_steps - q->steps) * q->dofs;
                 q->steps = done_steps;
                 const bool bad = rc != DGX_OK || st[i] != 0;
-                const bool done = !bad && (t[i] >= q->r.t_end || dt[i] == 0.0);
-                if (bad || done || q->cancel) {
-                    if (done) {
-                        dgx_conserved_totals(q->solver, q->totals, s->stream);
-                        q->t_final = t[i];
-                        if (q->r.keep_state) {
-                            q->result.resize(q->solver->s.n);
-                            dgx_get_state(q->solver, q->result.data());
-                        }
-                    }
-                    release_solve(s, q);
-                    if (q->cancel && !done) q->state = kCancelled;
-                    else finish(s, q, done ? kDone : kFailed, done ? DGX_OK : DGX_ERR_NONFINITE);
+                const bool fin = !bad && (t[i] >= q->r.t_end || dt[i] == 0.0);
+                if (fin) {
+                    done.push_back(q);
+                    t_done.push_back(t[i]);
+                } else if (bad || q->cancel) {
+                    leaving.push_back(q);
                 } else {
                     keep.push_back(q);
                 }
+            }
+        }
+        const int trc = retire_totals(s, done);
+        for (size_t j = 0; j < done.size() && !trc; ++j) {
+            Request *q = done[j];
+            q->t_final = t_done[j];
+            if (q->r.keep_state) {
+                q->result.resize(q->solver->s.n);
+                dgx_get_state(q->solver, q->result.data());
+            }
+        }
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            for (Request *q : done) {
+                release_solve(s, q);
+                if (trc) finish(s, q, kFailed, trc);
+                else finish(s, q, kDone, DGX_OK);
+            }
+            for (Request *q : leaving) {
+                release_solve(s, q);
+                if (q->cancel) q->state = kCancelled;
+                else finish(s, q, kFailed, DGX_ERR_NONFINITE);
             }
             if (keep.size() != n) {
                 s->active.swap(keep);
                 if (s->batch) dgx_batch_destroy(s->batch);
                 s->batch = nullptr;
+                evict_idle_meshes(s, 0, kIdleMeshes, std::set<MeshKey>());
             }
+            s->retire_s += std::chrono::duration<double>(Clock::now() - t1).count();
         }
     }
     if (s->batch) dgx_batch_destroy(s->batch);
     s->batch = nullptr;
+    cudaStreamSynchronize(s->stream);
     for (Request *q : s->active) release_solve(s, q);
     s->active.clear();
-    for (auto &kv : s->meshes) dgx_mesh_destroy(kv.second);
+    for (auto &kv : s->meshes)
+        if (kv.second.mesh) dgx_mesh_destroy(kv.second.mesh);
     s->meshes.clear();
+    s->mesh_bytes = 0;
+    if (s->red) cudaFree(s->red);
+    s->red = nullptr;
+    if (s->stage) cudaFreeHost(s->stage);
+    if (s->min_diam) cudaFreeHost(s->min_diam);
+    s->stage = nullptr;
+    s->min_diam = nullptr;
+    s->pool->trim();
     cudaStreamDestroy(s->stream);
 }
 
@@ -283,6 +517,9 @@ int dgx_server_create(size_t budget_bytes, int max_active, dgx_server **out) {
     if (!s) { set_error("host allocation failed"); return DGX_ERR_NOMEM; }
     s->budget = budget_bytes;
     s->max_active = max_active;
+    // released blocks kept for reuse: a quarter of the budget, at most 8 GiB
+    s->pool = new (std::nothrow) BlockPool(std::min(budget_bytes / 4, static_cast<size_t>(8) << 30));
+    if (!s->pool) { delete s; set_error("host allocation failed"); return DGX_ERR_NOMEM; }
     cudaGetDevice(&s->device);
     s->worker = std::thread(worker_main, s);
     *out = s;
@@ -293,7 +530,7 @@ int dgx_server_submit(dgx_server *s, const dgx_request *r, long long *id) {
     if (!s || !r) { set_error("NULL argument"); return DGX_ERR_INVALID; }
     int rc = validate(*r);
     if (rc) { set_error("invalid request"); return rc; }
-    if (estimate_bytes(*r, false) > s->budget) { set_error("request needs more device memory than the budget"); return DGX_ERR_BUSY; }
+    if (mesh_estimate(*r) + solver_estimate(*r) > s->budget) { set_error("request needs more device memory than the budget"); return DGX_ERR_BUSY; }
     Request *q = new (std::nothrow) Request();
     if (!q) { set_error("host allocation failed"); return DGX_ERR_NOMEM; }
     q->r = *r;
@@ -383,9 +620,13 @@ int dgx_server_get_stats(dgx_server *s, dgx_server_stats *out) {
     out->queued = static_cast<long long>(s->queue.size());
     out->dof_updates = s->dof_updates;
     out->busy_seconds = s->busy;
+    out->admit_seconds = s->admit_s;
+    out->repack_seconds = s->repack_s;
+    out->retire_seconds = s->retire_s;
+    out->idle_seconds = s->idle_s;
     out->repacks = s->repacks;
     out->steps = s->steps;
-    out->device_bytes_in_use = s->in_use;
+    out->device_bytes_in_use = s->in_use + s->mesh_bytes;
     if (!s->latencies.empty()) {
         std::vector<double> l = s->latencies;
         std::sort(l.begin(), l.end());
@@ -423,6 +664,7 @@ int dgx_server_destroy(dgx_server *s) {
     s->cv.notify_all();
     if (s->worker.joinable()) s->worker.join();
     for (auto &kv : s->all) delete kv.second;
+    delete s->pool;
     delete s;
     return DGX_OK;
 }

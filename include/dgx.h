@@ -370,6 +370,10 @@ typedef struct dgx_server_stats {
     double busy_seconds;         /* worker time spent stepping                          */
     double p50_latency_s, p99_latency_s, max_latency_s;   /* time-to-solution           */
     size_t device_bytes_in_use;  /* admitted footprint                                  */
+    double admit_seconds;        /* worker time spent creating admitted solves          */
+    double repack_seconds;       /* worker time spent rebuilding the batch              */
+    double retire_seconds;       /* worker time spent reading out and freeing finished solves */
+    double idle_seconds;         /* worker time spent waiting for requests              */
 } dgx_server_stats;
 /* budget_bytes: admission limit on the estimated device footprint of running
  * requests; max_active: slot limit. */

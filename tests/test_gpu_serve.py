@@ -62,7 +62,8 @@ def test_results_equal_alone_and_in_mix(gpu):
 
 def test_budget_admission_serialises_but_completes(gpu):
     sp = dict(specs()[0], n=6, order=1)
-    # a budget (64 KiB) that holds one of these solves (about 43 KiB) at a time
+    # a budget (64 KiB) that holds one of these solves (mesh and solver blocks,
+    # 48 KiB) at a time
     srv = Server(budget_bytes=64 << 10, max_active=64)
     ids = [srv.submit(request(**dict(sp, seed=sp["seed"] + i))) for i in range(4)]
     assert srv.wait_idle(120.0) == _ffi.OK
