@@ -10,9 +10,11 @@ mode x variable) advanced by one step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line.  ``--impl reference`` times the CPU restatement of the
-reference's per-edge / per-element loops (oracle/, FP64, all host threads) on
-a bounded sample of the same workload.  Under torchrun (N > 1) every rank runs
+Prints one JSON line.  ``--impl reference`` times the reference's own CPU
+Euler loops (built from its sources by oracle/Makefile; one serial process per
+host core) on a bounded sample of the same workload -- or, without the
+reference's sources, the CPU restatement in oracle/ -- and adds its CUDA solver
+rebuilt for sm_103a on the full workload (``reference_gpu``).  Under torchrun (N > 1) every rank runs
 an independent replica of the solve (the path has no data exchange between
 solves) and value is the sum over ranks.
 """
@@ -136,46 +138,105 @@ def build_mesh(n: int):
 
 
 def run_reference(args, rank, world):
-    """CPU restatement of the reference loops (FP64, OpenMP over all host cores)."""
+    """The reference's own implementations of the path, timed on this machine: its
+    CPU Euler loops (src/2d/conservation/euler/cpu, built from the reference's
+    sources by oracle/Makefile, serial, one process per host core on a bounded
+    sub-problem) give `value`; its CUDA Euler solver rebuilt for sm_103a
+    (oracle/ref_gpu_harness.cu around the reference's time_integrate_rk4) runs a
+    few steps of the full workload on the GPU (`reference_gpu`).  Without the
+    reference's sources the CPU figure falls back to the oracle port."""
     if rank != 0:
         return None
     from oracle import oracle as orc
     orc.build()
-    cores = orc.set_threads(os.cpu_count() or 1)
-    # size the per-step sample so that warm-up + timed steps take about two minutes
-    probe = build_mesh(64)
-    po = orc.Oracle(probe, 3, orc.EULER, orc.LLF, 1.4)
-    pc = po.project(orc.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
-    po.step(pc, po.cfl_dt(pc))
-    t0 = time.perf_counter()
-    po.step(pc, po.cfl_dt(pc))
-    per_elem = (time.perf_counter() - t0) / probe.num_elem
-    n_sample = 32
-    for n in (512, 256, 128, 64, 32):
-        if per_elem * 2 * n * n * (args.steps + args.warmup) <= 120.0:
-            n_sample = n
-            break
-    mesh = build_mesh(n_sample)
-    o = orc.Oracle(mesh, 3, orc.EULER, orc.LLF, 1.4)
-    c = o.project(orc.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
-    dofs = 4 * 10 * mesh.num_elem
-    for _ in range(args.warmup):
-        c = o.step(c, o.cfl_dt(c))
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        c = o.step(c, o.cfl_dt(c))
-    el = time.perf_counter() - t0
-    value = dofs * args.steps / el
-    sample = (f"{args.steps} RK4 steps of the same scheme (p=3 Euler, LLF, CFL) on a 2x{n_sample}^2 "
-              f"periodic sub-problem ({mesh.num_elem} elements) of the 2x1024^2 workload, FP64")
-    return {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload(args.mesh_n), "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
+    wave = (0.2, 1.0, 1.0, 1.0, 1.0)
+    out = {"metric": METRIC, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic", "config": workload(args.mesh_n), "impl": "reference"}
+    if orc.build_ref() is not None:
+        cores = os.cpu_count() or 1
+        # size each process's sub-problem so that the timed steps take about a minute
+        probe = build_mesh(16)
+        po = orc.Oracle(probe, 3, orc.EULER, orc.LLF, 1.4)
+        pc = po.project(orc.IC_DENSITY_WAVE, wave)
+        per_elem = orc.time_ref_cpu(probe, 3, pc, po.cfl_dt(pc), 4)[0] / (4 * probe.num_elem)
+        n_sample = 8
+        for n in (256, 128, 64, 32, 16, 8):
+            if per_elem * 2 * n * n * args.steps <= 60.0:
+                n_sample = n
+                break
+        mesh = build_mesh(n_sample)
+        o = orc.Oracle(mesh, 3, orc.EULER, orc.LLF, 1.4)
+        c = o.project(orc.IC_DENSITY_WAVE, wave)
+        secs = orc.time_ref_cpu(mesh, 3, c, o.cfl_dt(c), args.steps, procs=cores)
+        dofs = 4 * 10 * mesh.num_elem
+        el = max(secs)
+        value = cores * dofs * args.steps / el
+        kind = "reference"
+        sample = (f"{args.steps} RK4 steps of the reference's own CPU Euler loops (serial FP64 C, "
+                  f"built from its sources) on a 2x{n_sample}^2 periodic sub-problem ({mesh.num_elem} "
+                  f"elements, p=3 density wave) of the 2x1024^2 workload, in {cores} processes side by "
+                  f"side (one per host core)")
+    else:
+        cores = orc.set_threads(os.cpu_count() or 1)
+        # size the per-step sample so that warm-up + timed steps take about two minutes
+        probe = build_mesh(64)
+        po = orc.Oracle(probe, 3, orc.EULER, orc.LLF, 1.4)
+        pc = po.project(orc.IC_DENSITY_WAVE, wave)
+        po.step(pc, po.cfl_dt(pc))
+        t0 = time.perf_counter()
+        po.step(pc, po.cfl_dt(pc))
+        per_elem = (time.perf_counter() - t0) / probe.num_elem
+        n_sample = 32
+        for n in (512, 256, 128, 64, 32):
+            if per_elem * 2 * n * n * (args.steps + args.warmup) <= 120.0:
+                n_sample = n
+                break
+        mesh = build_mesh(n_sample)
+        o = orc.Oracle(mesh, 3, orc.EULER, orc.LLF, 1.4)
+        c = o.project(orc.IC_DENSITY_WAVE, wave)
+        dofs = 4 * 10 * mesh.num_elem
+        for _ in range(args.warmup):
+            c = o.step(c, o.cfl_dt(c))
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            c = o.step(c, o.cfl_dt(c))
+        el = time.perf_counter() - t0
+        value = dofs * args.steps / el
+        kind = "port"
+        sample = (f"{args.steps} RK4 steps of the same scheme (p=3 Euler, LLF, CFL) on a 2x{n_sample}^2 "
+                  f"periodic sub-problem ({mesh.num_elem} elements) of the 2x1024^2 workload, FP64")
+    out.update({"value": value, "ms_per_step": 1e3 * el / args.steps,
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    out["reference_gpu"] = run_reference_gpu(args.mesh_n)
+    return out
+
+
+def run_reference_gpu(mesh_n: int, steps: int = 3):
+    """The reference's CUDA Euler solver (FP64, its own kernels and host loop,
+    rebuilt for sm_103a) on the full workload: `steps` steps of its
+    time_integrate_rk4 to an end time of `steps` CFL time steps."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no GPU"}
+        from oracle import ref_gpu
+        if ref_gpu.build() is None:
+            return {"unavailable": "the reference's CUDA sources are not at hand to build its solver"}
+        from oracle import oracle as orc
+        mesh = build_mesh(mesh_n)
+        o = orc.Oracle(mesh, 3, orc.EULER, orc.LLF, 1.4)
+        c0 = o.project(orc.IC_DENSITY_WAVE, (0.2, 1.0, 1.0, 1.0, 1.0))
+        dt = o.cfl_dt(c0)
+        r = ref_gpu.run(mesh, 3, c0, steps * dt * 0.999)
+        dofs = 4 * 10 * mesh.num_elem
+        return {"value": dofs * r["steps"] / r["seconds"], "unit": UNIT, "steps": r["steps"],
+                "ms_per_step": 1e3 * r["seconds"] / r["steps"], "dtype": "f64",
+                "what": "the reference's own CUDA kernels and RK4 host loop (time_integrate_rk4) rebuilt "
+                        f"for sm_103a, 2x{mesh_n}^2 density wave p=3, wall time of the loop"}
+    except Exception as exc:  # reported, never fatal to the bench line
+        return {"unavailable": f"{type(exc).__name__}: {exc}"[:300]}
 
 
 def cpu_baseline_sample(budget_s: float = 12.0):

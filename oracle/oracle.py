@@ -35,12 +35,55 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref(reference_root: str = "/root/reference") -> str | None:
-    """Compile the reference's own CPU Euler loops (needs the reference tree)."""
+def install_ref(reference_root: str = "/root/reference") -> bool:
+    """Copy the reference's Euler sources the harnesses compile (unmodified) to
+    baseline/_ref/src/2d, for machines without the reference tree."""
     if not os.path.isdir(reference_root):
-        return None
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={reference_root}"], check=True)
-    return REF_BIN
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref-src", f"REF={reference_root}"], check=True)
+    return True
+
+
+def build_ref(reference_root: str = "/root/reference") -> str | None:
+    """Compile the reference's own CPU Euler loops, from the reference tree or
+    the installed copy; the binary path or None."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={reference_root}"],
+                       capture_output=True, text=True)
+    return REF_BIN if r.returncode == 0 and os.path.exists(REF_BIN) else None
+
+
+def time_ref_cpu(mesh, p: int, c0, dt: float, nsteps: int, procs: int = 1) -> list:
+    """Wall seconds of `nsteps` RK4 steps of the reference's own CPU Euler loops
+    (oracle/_ref/ref_euler, fixed dt) on `mesh` from c0, in `procs` processes
+    run side by side (the reference's loops are serial); one figure per process."""
+    ref_bin = build_ref()
+    if ref_bin is None:
+        raise RuntimeError("the reference's CPU loops are not built (no reference sources)")
+    import tempfile
+    E, S = mesh.num_elem, mesh.num_sides
+    with tempfile.TemporaryDirectory() as td:
+        fin = os.path.join(td, "in.bin")
+        with open(fin, "wb") as f:
+            np.array([E, S, p, nsteps, 0, 1, 0, 0], dtype=np.int32).tofile(f)
+            np.array([dt], dtype=np.float64).tofile(f)
+            for a in mesh.vertices():
+                np.asarray(a, dtype=np.float64).tofile(f)
+            for a in mesh.elem_sides():
+                np.asarray(a, dtype=np.int32).tofile(f)
+            for a in mesh.side_arrays():
+                np.asarray(a, dtype=np.int32).tofile(f)
+            np.asarray(c0, dtype=np.float64).tofile(f)
+        outs = [os.path.join(td, f"out{k}.bin") for k in range(procs)]
+        ps = [subprocess.Popen([ref_bin, fin, o], stdout=subprocess.DEVNULL) for o in outs]
+        codes = [q.wait() for q in ps]
+        if any(codes):
+            raise RuntimeError(f"reference CPU loops failed: exit codes {codes}")
+        secs = []
+        for o in outs:
+            with open(o, "rb") as f:
+                f.seek(-8, os.SEEK_END)
+                secs.append(float(np.frombuffer(f.read(8), dtype=np.float64)[0]))
+    return secs
 
 
 def lib():

@@ -1,0 +1,66 @@
+"""TEST INFRASTRUCTURE ONLY: the reference's own CUDA Euler solver as a checker
+and a reported baseline, never as the product path.
+
+`oracle/_ref/ref_gpu_euler` is built by `make -C oracle ref-gpu` from the
+reference's unmodified sources (src/2d/conservation and src/2d/{quadrature,
+basis}.cu, from the reference tree or the copy `make -C oracle ref-src` installs
+under baseline/_ref) with `ref_gpu_harness.cu` as its problem file and driver.
+`run` hands it a periodic mesh and an initial state, lets the reference's own
+time_integrate_rk4 (src/2d/conservation/time_integrator.cu:221-434) advance to
+t_end with its CFL rule, and returns the state, the steps taken and the time.
+"""
+from __future__ import annotations
+
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BIN = os.path.join(HERE, "_ref", "ref_gpu_euler")
+
+
+def build() -> str | None:
+    """Build the harness if its sources are at hand; the binary path or None."""
+    if not os.path.exists(BIN):
+        r = subprocess.run(["make", "-s", "-C", HERE, "ref-gpu"], capture_output=True, text=True)
+        if r.returncode != 0:
+            return None
+    return BIN if os.path.exists(BIN) else None
+
+
+def run(mesh, order: int, c0: np.ndarray, t_end: float, timeout: float = 900.0) -> dict:
+    """Advance the Euler state c0 (layout c[4][Np][E], FP64) on `mesh` (a
+    dgcuda_gb300.mesh.Mesh, periodic) to t_end with the reference's solver."""
+    binp = build()
+    if binp is None:
+        raise RuntimeError("the reference's CUDA solver is not built (no reference sources)")
+    E, S = mesh.num_elem, mesh.num_sides
+    npm = (order + 1) * (order + 2) // 2
+    c0 = np.ascontiguousarray(c0, dtype=np.float64).reshape(-1)
+    if c0.size != 4 * npm * E:
+        raise ValueError("c0 must hold 4 * Np * E values")
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        with open(fin, "wb") as f:
+            f.write(struct.pack("<4i", E, S, order, 0))
+            f.write(struct.pack("<d", float(t_end)))
+            for a in mesh.vertices():
+                f.write(np.ascontiguousarray(a, dtype="<f8").tobytes())
+            for a in mesh.elem_sides():
+                f.write(np.ascontiguousarray(a, dtype="<i4").tobytes())
+            for a in mesh.side_arrays():
+                f.write(np.ascontiguousarray(a, dtype="<i4").tobytes())
+            f.write(c0.astype("<f8").tobytes())
+        r = subprocess.run([binp, fin, fout], capture_output=True, text=True, timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference solver failed ({r.returncode}): {r.stderr.strip()[-400:]}")
+        with open(fout, "rb") as f:
+            steps, _ = struct.unpack("<2i", f.read(8))
+            secs, min_r = struct.unpack("<2d", f.read(16))
+            c = np.frombuffer(f.read(), dtype="<f8").copy()
+    if c.size != c0.size:
+        raise RuntimeError("reference solver wrote a short state")
+    return {"state": c, "steps": steps, "seconds": secs, "min_r": min_r}

@@ -20,11 +20,13 @@
  * (time_integrator_euler.c:289-356) in the order of time_integrate_fe
  * (:359-406), also with a fixed dt.
  *
- * Input file (little-endian): int32[8] {num_elem, num_sides, p, nsteps, fe_steps, 0...},
+ * Input file (little-endian): int32[8] {num_elem, num_sides, p, nsteps, fe_steps, timed, 0...},
  * float64 dt, float64 V1x..V3y[E] (6 arrays), int32 elem_s1..3[E],
  * int32 left_elem, right_elem, left_side, right_side [S], float64 c0[4*Np*E].
- * Output file: see write order in main() below.
+ * Output file: see write order in main() below; with `timed` set, the wall
+ * time of the RK4 steps (double, seconds) closes it.
  */
+#include <time.h>
 #include "euler.c"
 
 static void *xread(FILE *f, size_t n) {
@@ -39,7 +41,9 @@ static void xwrite(FILE *f, const void *p, size_t n) {
 
 int main(int argc, char *argv[]) {
     FILE *in, *out;
-    int hdr[8], E, S, n, n_p, nsteps, fe_steps, i, step;
+    int hdr[8], E, S, n, n_p, nsteps, fe_steps, timed, i, step;
+    struct timespec ts0, ts1;
+    double rk4_seconds;
     double dt;
     double *V[6];
     int *es[3], *le, *re, *lsn, *rsn;
@@ -52,7 +56,7 @@ int main(int argc, char *argv[]) {
     in = fopen(argv[1], "rb");
     if (!in) return 1;
     if (fread(hdr, sizeof(int), 8, in) != 8) return 2;
-    E = hdr[0]; S = hdr[1]; n = hdr[2]; nsteps = hdr[3]; fe_steps = hdr[4];
+    E = hdr[0]; S = hdr[1]; n = hdr[2]; nsteps = hdr[3]; fe_steps = hdr[4]; timed = hdr[5];
     n_p = (n + 1) * (n + 2) / 2;
     if (fread(&dt, sizeof(double), 1, in) != 1) return 2;
     for (i = 0; i < 6; i++) V[i] = (double *)xread(in, sizeof(double) * E);
@@ -131,6 +135,7 @@ int main(int argc, char *argv[]) {
     xwrite(out, d_k1, sizeof(double) * NV);
 
     /* nsteps classic RK4 steps with a fixed dt, stage order of time_integrate_rk4 */
+    clock_gettime(CLOCK_MONOTONIC, &ts0);
     for (step = 0; step < nsteps; step++) {
         double *ks[4] = {d_k1, d_k2, d_k3, d_k4};
         double alpha[3] = {0.5, 0.5, 1.0};
@@ -147,6 +152,8 @@ int main(int argc, char *argv[]) {
         }
         rk4(d_c, d_k1, d_k2, d_k3, d_k4, n_p, E);
     }
+    clock_gettime(CLOCK_MONOTONIC, &ts1);
+    rk4_seconds = (double)(ts1.tv_sec - ts0.tv_sec) + 1e-9 * (double)(ts1.tv_nsec - ts0.tv_nsec);
     xwrite(out, d_c, sizeof(double) * NV);
 
     /* fe_steps forward-Euler steps from the initial state */
@@ -162,6 +169,7 @@ int main(int argc, char *argv[]) {
         }
         xwrite(out, d_c, sizeof(double) * NV);
     }
+    if (timed) xwrite(out, &rk4_seconds, sizeof(rk4_seconds));
     fclose(out);
     return 0;
 }
