@@ -1,13 +1,17 @@
-"""TEST INFRASTRUCTURE ONLY: the reference's own CUDA Euler solver as a checker
-and a reported baseline, never as the product path.
+"""TEST INFRASTRUCTURE ONLY: the reference's own CUDA solvers as checkers and a
+reported baseline, never as the product path.
 
-`oracle/_ref/ref_gpu_euler` is built by `make -C oracle ref-gpu` from the
-reference's unmodified sources (src/2d/conservation and src/2d/{quadrature,
-basis}.cu, from the reference tree or the copy `make -C oracle ref-src` installs
-under baseline/_ref) with `ref_gpu_harness.cu` as its problem file and driver.
-`run` hands it a periodic mesh and an initial state, lets the reference's own
-time_integrate_rk4 (src/2d/conservation/time_integrator.cu:221-434) advance to
-t_end with its CFL rule, and returns the state, the steps taken and the time.
+`oracle/_ref/ref_gpu_euler` and `ref_gpu_advec` are built by `make -C oracle
+ref-gpu` from the reference's unmodified sources (src/2d/conservation,
+src/2d/2dadvec and src/2d/{time_integrator,quadrature,basis}.cu, from the
+reference tree or the copy `make -C oracle ref-src` installs under
+baseline/_ref) with `ref_gpu_harness.cu` as their problem file and driver.
+`run` hands the Euler solver a periodic mesh and an initial state and lets the
+reference's time_integrate_rk4 (src/2d/conservation/time_integrator.cu:221-434)
+advance to t_end with its CFL rule; `run_advection` lets the advection solver's
+time_integrate_rk4 (src/2d/time_integrator.cu:89-315) take a number of steps of
+a fixed dt (a = (1,1), central flux).  Both return the state, the steps taken
+and the time.
 """
 from __future__ import annotations
 
@@ -20,33 +24,45 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BIN = os.path.join(HERE, "_ref", "ref_gpu_euler")
+BIN_ADVEC = os.path.join(HERE, "_ref", "ref_gpu_advec")
 
 
 def build() -> str | None:
-    """Build the harness if its sources are at hand; the binary path or None."""
-    if not os.path.exists(BIN):
+    """Build the harnesses if their sources are at hand; the Euler binary's path
+    or None."""
+    if not (os.path.exists(BIN) and os.path.exists(BIN_ADVEC)):
         r = subprocess.run(["make", "-s", "-C", HERE, "ref-gpu"], capture_output=True, text=True)
         if r.returncode != 0:
             return None
-    return BIN if os.path.exists(BIN) else None
+    return BIN if os.path.exists(BIN) and os.path.exists(BIN_ADVEC) else None
 
 
 def run(mesh, order: int, c0: np.ndarray, t_end: float, timeout: float = 900.0) -> dict:
     """Advance the Euler state c0 (layout c[4][Np][E], FP64) on `mesh` (a
     dgcuda_gb300.mesh.Mesh, periodic) to t_end with the reference's solver."""
-    binp = build()
-    if binp is None:
-        raise RuntimeError("the reference's CUDA solver is not built (no reference sources)")
+    return _run(BIN, mesh, order, c0, 4, 0, t_end, timeout)
+
+
+def run_advection(mesh, order: int, c0: np.ndarray, dt: float, steps: int, timeout: float = 900.0) -> dict:
+    """`steps` RK4 steps of dt of the advection state c0 (c[Np][E], FP64) on
+    `mesh` (periodic) with the reference's advection solver (a = (1,1))."""
+    return _run(BIN_ADVEC, mesh, order, c0, 1, int(steps), dt, timeout)
+
+
+def _run(binary, mesh, order, c0, nv, steps, t_in, timeout):
+    if build() is None:
+        raise RuntimeError("the reference's CUDA solvers are not built (no reference sources)")
+    binp = binary
     E, S = mesh.num_elem, mesh.num_sides
     npm = (order + 1) * (order + 2) // 2
     c0 = np.ascontiguousarray(c0, dtype=np.float64).reshape(-1)
-    if c0.size != 4 * npm * E:
-        raise ValueError("c0 must hold 4 * Np * E values")
+    if c0.size != nv * npm * E:
+        raise ValueError(f"c0 must hold {nv} * Np * E values")
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
-            f.write(struct.pack("<4i", E, S, order, 0))
-            f.write(struct.pack("<d", float(t_end)))
+            f.write(struct.pack("<4i", E, S, order, steps))
+            f.write(struct.pack("<d", float(t_in)))
             for a in mesh.vertices():
                 f.write(np.ascontiguousarray(a, dtype="<f8").tobytes())
             for a in mesh.elem_sides():

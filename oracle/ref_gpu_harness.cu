@@ -1,18 +1,24 @@
 // ref_gpu_harness.cu -- TEST INFRASTRUCTURE ONLY (a checker and a reported
 // baseline, never the product path).
 //
-// Runs the reference's own CUDA Euler solver, compiled from its unmodified
-// sources (src/2d/conservation: conserv.cu, conserv_kernels.cu,
-// conserv_kernels_wrappers.cu, time_integrator.cu, euler/euler.cu and
-// src/2d/{quadrature,basis}.cu, all included below), on a mesh and initial
-// state given in a binary file, and writes the state it reaches.  This file
-// plays the part of the reference's problem file
-// (src/2d/conservation/euler/supersonic/supersonic.cu:1-124): it defines the
-// physics hooks and a driver that repeats run_dgcuda's set-up
-// (src/2d/conservation/main.cu:54-170) with the arrays filled directly instead
-// of read_mesh, sets the initial coefficients directly instead of
-// init_conditions, and calls the reference's own time_integrate_rk4
-// (src/2d/conservation/time_integrator.cu:221-434) unchanged.
+// Runs the reference's own CUDA solvers, compiled from its unmodified sources,
+// on a mesh and initial state given in a binary file, and writes the state they
+// reach.  Built twice (oracle/Makefile):
+//  * Euler (default): src/2d/conservation (conserv.cu, conserv_kernels.cu,
+//    conserv_kernels_wrappers.cu, time_integrator.cu, main.cu, euler/euler.cu)
+//    and src/2d/{quadrature,basis}.cu.  This file plays the part of the
+//    reference's problem file (src/2d/conservation/euler/supersonic/
+//    supersonic.cu:1-124): the physics hooks, and a driver that repeats
+//    run_dgcuda's set-up (src/2d/conservation/main.cu:54-170) with the arrays
+//    filled directly instead of read_mesh and the initial coefficients set
+//    directly instead of init_conditions, then calls the reference's own
+//    time_integrate_rk4 (src/2d/conservation/time_integrator.cu:221-434)
+//    unchanged (CFL time step, run to t_end).
+//  * Advection (-DREF_ADVECTION): src/2d/2dadvec (2dadvec.cu with its kernels
+//    and wrappers) and src/2d/{time_integrator,quadrature,basis}.cu.  The
+//    driver repeats src/2d/main.cu:40-196 the same way and calls that
+//    time_integrate_rk4 (src/2d/time_integrator.cu:89-315) unchanged (fixed dt,
+//    a number of steps).
 //
 // Three build adaptations, made here rather than in the reference's files:
 //  * cudaThreadSynchronize (removed in CUDA 13) maps to cudaDeviceSynchronize;
@@ -21,17 +27,18 @@
 //  * __syncthreads() compiles to nothing.  The reference calls it inside
 //    `if (idx < n)` blocks of its per-side and per-element kernels, which use
 //    no shared memory: a barrier some threads of a block never reach.  Its only
-//    kernels with shared memory, min_reduction and max_reduction, are not
-//    called (run_dgcuda also takes the minimum radius on the host).
-// printf is routed to a counter: the time loop prints "\rt = ..." once per
-// step, which gives the number of steps taken.
+//    kernels with shared memory, the min/max reductions, are not called (the
+//    set-up takes the minimum radius on the host, as run_dgcuda does).
+// printf is routed to a counter: the Euler time loop prints "\rt = ..." once
+// per step, which gives the number of steps taken.
 //
-// Usage: ref_gpu_euler <in.bin> <out.bin>
-//   in:  int32 E, S, p, 0; double t_end; double V[6][E] (V1x V1y V2x V2y V3x V3y);
-//        int32 elem_s[3][E]; int32 sides[4][S] (left_elem right_elem
-//        left_side right_side); double c[4][Np][E]
+// Usage: ref_gpu_euler|ref_gpu_advec <in.bin> <out.bin>
+//   in:  int32 E, S, p, steps; double t (Euler: end time; advection: dt);
+//        double V[6][E] (V1x V1y V2x V2y V3x V3y); int32 elem_s[3][E];
+//        int32 sides[4][S] (left_elem right_elem left_side right_side);
+//        double c[NV][Np][E] (NV = 4 Euler, 1 advection)
 //   out: int32 steps, 0; double seconds (time_integrate_rk4, wall clock),
-//        min_r; double c[4][Np][E]
+//        min_r (Euler; 0 for advection); double c[NV][Np][E]
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -60,10 +67,18 @@ static int ref_printf(const char *fmt, ...) {
 
 #define printf ref_printf
 #define __syncthreads() ((void)0)
-#include "euler/euler.cu"
+#if REF_ADVECTION
+#include "2dadvec/2dadvec.cu"
+#else
+#include "conservation/euler/euler.cu"
+#endif
 #undef __syncthreads
 #undef printf
 
+#if REF_ADVECTION
+constexpr int kVars = 1;
+#else
+constexpr int kVars = 4;
 // ---- the problem: periodic meshes only, gamma 1.4 -------------------------
 int limiter = NO_LIMITER;
 int time_integrator = RK4;
@@ -87,10 +102,14 @@ __device__ void reflecting_boundary(double *U_left, double *U_right, double v1x,
     (void)nx; (void)ny; (void)j; (void)left_side; (void)n_quad1d;
 }
 
+#endif
+
 static cudaError_t ref_symbol_copy(const char *name, const void *src, size_t count) {
 #define REF_SYMBOL(s) \
     if (std::strcmp(name, #s) == 0) return cudaMemcpyToSymbol(s, src, count);
+#if !REF_ADVECTION
     REF_SYMBOL(N)
+#endif
     REF_SYMBOL(basis)
     REF_SYMBOL(basis_grad_x)
     REF_SYMBOL(basis_grad_y)
@@ -120,13 +139,13 @@ int main(int argc, char **argv) {
     FILE *fi = std::fopen(argv[1], "rb");
     if (!fi) { std::fprintf(stderr, "cannot open %s\n", argv[1]); return 2; }
     int hdr[4];
-    double t_end = 0.0;
-    if (std::fread(hdr, sizeof(int), 4, fi) != 4 || std::fread(&t_end, sizeof(double), 1, fi) != 1) {
+    double t_in = 0.0;   // Euler: end time; advection: dt
+    if (std::fread(hdr, sizeof(int), 4, fi) != 4 || std::fread(&t_in, sizeof(double), 1, fi) != 1) {
         std::fprintf(stderr, "bad header\n");
         return 2;
     }
-    const int num_elem = hdr[0], num_sides = hdr[1], n = hdr[2];
-    if (num_elem <= 0 || num_sides <= 0 || n < 0 || n > 5 || !(t_end > 0.0)) {
+    const int num_elem = hdr[0], num_sides = hdr[1], n = hdr[2], timesteps = hdr[3];
+    if (num_elem <= 0 || num_sides <= 0 || n < 0 || n > 5 || !(t_in > 0.0) || (REF_ADVECTION && timesteps < 1)) {
         std::fprintf(stderr, "bad sizes\n");
         return 2;
     }
@@ -135,7 +154,7 @@ int main(int argc, char **argv) {
     std::vector<double> V, c0;
     std::vector<int> es, sd;
     if (!read_vec(fi, V, 6 * E) || !read_vec(fi, es, 3 * E) || !read_vec(fi, sd, 4 * S) ||
-        !read_vec(fi, c0, 4 * n_p * E)) {
+        !read_vec(fi, c0, kVars * n_p * E)) {
         std::fprintf(stderr, "short input\n");
         return 2;
     }
@@ -165,29 +184,39 @@ int main(int argc, char **argv) {
         sy2[s] = vy[(k + 1) % 3];
     }
 
-    // run_dgcuda's set-up (main.cu:68-163)
+    // the reference driver's set-up (Euler: conservation/main.cu:68-163;
+    // advection: src/2d/main.cu:101-186)
     init_gpu(num_elem, num_sides, n_p, V1x, V1y, V2x, V2y, V3x, V3y, left_side_number, right_side_number,
              sx1.data(), sy1.data(), sx2.data(), sy2.data(), elem_s1, elem_s2, elem_s3, left_elem, right_elem);
-    set_N(local_N);
     checkCudaError("error after gpu init.");
+#if REF_ADVECTION
+    const int n_threads = 128;
+#else
+    set_N(local_N);
     const int n_threads = 256;
+#endif
     const int n_blocks_elem = (num_elem / n_threads) + ((num_elem % n_threads) ? 1 : 0);
     const int n_blocks_sides = (num_sides / n_threads) + ((num_sides % n_threads) ? 1 : 0);
+    double min_r = 0.0;
+#if !REF_ADVECTION
     preval_inscribed_circles<<<n_blocks_elem, n_threads>>>(d_J, d_V1x, d_V1y, d_V2x, d_V2y, d_V3x, d_V3y, num_elem);
     std::vector<double> radius(E);
     cudaMemcpy(radius.data(), d_J, E * sizeof(double), cudaMemcpyDeviceToHost);
-    double min_r = radius[0];
+    min_r = radius[0];
     for (size_t i = 1; i < E; ++i) min_r = radius[i] < min_r ? radius[i] : min_r;
+#endif
     preval_jacobian<<<n_blocks_elem, n_threads>>>(d_J, d_V1x, d_V1y, d_V2x, d_V2y, d_V3x, d_V3y, num_elem);
     cudaDeviceSynchronize();
     preval_side_length<<<n_blocks_sides, n_threads>>>(d_s_length, d_s_V1x, d_s_V1y, d_s_V2x, d_s_V2y, num_sides);
     preval_normals<<<n_blocks_sides, n_threads>>>(d_Nx, d_Ny, d_s_V1x, d_s_V1y, d_s_V2x, d_s_V2y, d_V1x, d_V1y,
                                                   d_V2x, d_V2y, d_V3x, d_V3y, d_left_side_number, num_sides);
     cudaDeviceSynchronize();
+#if !REF_ADVECTION
     cudaFree(d_s_V1x);
     cudaFree(d_s_V2x);
     cudaFree(d_s_V1y);
     cudaFree(d_s_V2y);
+#endif
     preval_normals_direction<<<n_blocks_sides, n_threads>>>(d_Nx, d_Ny, d_V1x, d_V1y, d_V2x, d_V2y, d_V3x, d_V3y,
                                                             d_left_elem, d_left_side_number, num_sides);
     preval_partials<<<n_blocks_elem, n_threads>>>(d_V1x, d_V1y, d_V2x, d_V2y, d_V3x, d_V3y, d_xr, d_yr, d_xs, d_ys,
@@ -205,7 +234,12 @@ int main(int argc, char **argv) {
 
     cudaDeviceSynchronize();
     const auto t0 = std::chrono::steady_clock::now();
-    time_integrate_rk4(n_quad, n_quad1d, n_p, n, num_elem, num_sides, t_end, min_r);
+#if REF_ADVECTION
+    time_integrate_rk4(t_in, n_quad, n_quad1d, n_p, n, num_elem, num_sides, 0, 0, timesteps);
+    g_steps = timesteps;
+#else
+    time_integrate_rk4(n_quad, n_quad1d, n_p, n, num_elem, num_sides, t_in, min_r);
+#endif
     cudaDeviceSynchronize();
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     checkCudaError("error after time integration.");

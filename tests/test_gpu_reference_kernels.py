@@ -1,6 +1,15 @@
-"""Parity with the reference's own CUDA Euler solver, rebuilt for sm_103a and
-run on the same GPU (oracle/ref_gpu_harness.cu drives the reference's
-time_integrate_rk4, src/2d/conservation/time_integrator.cu:221-434, unchanged).
+"""Parity with the reference's own CUDA solvers, rebuilt for sm_103a and run on
+the same GPU (oracle/ref_gpu_harness.cu drives the reference's Euler
+time_integrate_rk4, src/2d/conservation/time_integrator.cu:221-434, and its
+advection time_integrate_rk4, src/2d/time_integrator.cu:89-315, unchanged).
+
+Advection: the reference hard-wires a = (1,1) and the central flux
+(src/2d/2dadvec/2dadvec_kernels.cu:150-164); both sides take the same number of
+steps of the same fixed dt from the same FP64 coefficients.  Its side lengths
+and normals also use float square roots.  Tolerances: FP64 path <= 1e-9, FP32
+path <= 1e-5.
+
+Euler:
 
 Both sides start from the same FP64 coefficients and advance to the same end
 time with the same CFL rule (dt = 0.7 min_d / max lambda / (2p+1), the last step
@@ -80,3 +89,34 @@ def test_paths_match_reference_gpu_solver(ref_gpu, case):
     print(f"{case[0]}: {ref['steps']} steps, FP64 vs reference {err64:.2e}, FP32 vs reference {err32:.2e}")
     assert err64 <= 1e-9, err64
     assert err32 <= 1e-5, err32
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4])
+def test_advection_matches_reference_gpu_solver(ref_gpu, p):
+    n = 16
+    mesh = periodic_square(n, jitter=0.15, seed=40 + p)
+    init = Solver(mesh, p, _ffi.ADVECTION, _ffi.FLUX_CENTRAL, _ffi.FP64)
+    init.project(_ffi.IC_GAUSSIAN, (0.4, 0.6, 0.02, 1.0, 1.0))
+    c0 = init.get_state()
+    init.close()
+    dt = 0.1 * (1.0 / n) / (np.sqrt(2.0) * (2 * p + 1))
+    steps = 25
+    ref = ref_gpu.run_advection(mesh, p, c0, dt, steps)
+    assert ref["steps"] == steps
+    assert np.all(np.isfinite(ref["state"]))
+    moved = np.linalg.norm(ref["state"] - c0.reshape(-1)) / np.linalg.norm(c0)
+    assert moved > 1e-3, "the reference solver did not move the state"
+    errs = {}
+    for name, prec in (("fp64", _ffi.FP64), ("fp32", _ffi.FP32)):
+        sv = Solver(mesh, p, _ffi.ADVECTION, _ffi.FLUX_CENTRAL, prec)
+        sv.set_state(c0)
+        sv.set_dt(dt)
+        k, _ = sv.run(max_steps=steps)
+        assert k == steps
+        s_ = sv.get_state().reshape(-1)
+        sv.close()
+        errs[name] = np.linalg.norm(s_ - ref["state"]) / np.linalg.norm(ref["state"])
+    print(f"advection p={p}: {steps} steps, FP64 vs reference {errs['fp64']:.2e}, "
+          f"FP32 vs reference {errs['fp32']:.2e}")
+    assert errs["fp64"] <= 1e-9, errs
+    assert errs["fp32"] <= 1e-5, errs
