@@ -461,9 +461,268 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
     return pre;
 }
 
+#ifndef DGX_PAIRED
+#define DGX_PAIRED 1
+#endif
+
+// Pairs of values: for FP32, two fused multiply-adds in one instruction
+// (sm_100 and later), each lane bitwise fmaf(a, b, c); FP64 (never paired by
+// the kernels) has the scalar form so that the code compiles for both.
+template <typename T> struct Pair2;
+template <> struct Pair2<float> { using type = float2; };
+template <> struct Pair2<double> { using type = double2; };
+using R2 = typename Pair2<R>::type;
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ double2 fma2(double2 a, double2 b, double2 c) {
+    return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
+}
+__device__ __forceinline__ R2 mk2(R x, R y) { R2 v; v.x = x; v.y = y; return v; }
+__device__ __forceinline__ R2 dup2(R t) { return mk2(t, t); }
+
+// FP32 Euler: stage_tile with the four variables held as the pairs
+// (rho, rho u) and (rho v, E), so that every basis contraction (traces, point
+// values, volume projection, lift) issues one paired FMA per two variables.
+// Each lane performs the scalar kernel's fused multiply-adds with the same
+// operands in the same order, so the results are bitwise stage_tile's; the
+// fluxes and the epilogue stay scalar.
+template <int P, bool BND>
+__device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int tile, unsigned char *smem_raw,
+                                                const unsigned parity) {
+    using L = Lay<P>;
+    constexpr int NP = L::NP, NQ = L::NQ, NQ1 = L::NQ1;
+    constexpr int EQ = DGX_EULER, NV = 4;
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem_raw);
+    R *s_side = reinterpret_cast<R *>(smem_raw + 16);
+    R *s_tr = s_side + side_table_words<P, NV>();
+    const int nslot = a.nslot;
+    constexpr int TSW = slot_words<P, NV>();
+    R *s_pre = s_tr + static_cast<size_t>(TSW) * nslot;
+
+    R dt;
+    if (a.mode == 0) {
+        dt = R(a.dt);
+    } else {
+        dt = R(a.scal[0]);
+        if (dt == R(0)) return false;   // the run has reached its end time (uniform over the CTA)
+    }
+    const int E = a.E;
+    const int tid = threadIdx.x;
+    const int e = tile * kTile + tid;
+    const bool live = e < E;
+    const size_t SE = static_cast<size_t>(E);
+    const R g = a.gammaf, ax = a.axf, ay = a.ayf;
+    const int llf = a.flux == DGX_FLUX_LLF;
+    const R *__restrict__ u = static_cast<const R *>(a.u);
+
+    for (int t = tid; t < 3 * NP * NQ1; t += kTile) s_side[t] = c_tab[L::SIDE + t];
+    const bool pre = issue_prefetch<P, NV>(a, tile, bar, s_pre, tid);
+
+    R2 c2[2][NP];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+            c2[h][i] = live ? mk2(__ldg(u + ((2 * h) * NP + i) * SE + e), __ldg(u + ((2 * h + 1) * NP + i) * SE + e))
+                            : mk2(R(0), R(0));
+
+    int sw[3];
+    R snx[3], sny[3], shl[3];
+    {
+        const int *__restrict__ nbr = a.nbr;
+        const R *__restrict__ fn = static_cast<const R *>(a.fn);
+        const int ee = live ? e : 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            sw[k] = __ldg(nbr + k * SE + ee);
+            snx[k] = __ldg(fn + (3 * k + 0) * SE + ee);
+            sny[k] = __ldg(fn + (3 * k + 1) * SE + ee);
+            shl[k] = __ldg(fn + (3 * k + 2) * SE + ee);
+        }
+    }
+
+    const int h0 = __ldg(a.halo_off + tile), H = __ldg(a.halo_off + tile + 1) - h0;
+    R2 cn2[2][NP];
+    int hw = tid < H ? __ldg(a.halo_list + h0 + tid) : -1;
+    if (hw >= 0) {
+        const int ne = hw >> 2;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int i = 0; i < NP; ++i)
+                cn2[h][i] = mk2(__ldg(u + ((2 * h) * NP + i) * SE + ne), __ldg(u + ((2 * h + 1) * NP + i) * SE + ne));
+    }
+
+    // own traces on the three sides (constant-bank side tables)
+#if DGX_ROLLED_TRACES
+#pragma unroll 1
+#else
+#pragma unroll
+#endif
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                R2 s2 = mk2(R(0), R(0));
+#pragma unroll
+                for (int i = 0; i < NP; ++i) s2 = fma2(c2[h][i], dup2(c_tab[L::SIDE + (k * NP + i) * NQ1 + j]), s2);
+                s_tr[(3 * tid + k) * TSW + j * NV + 2 * h] = s2.x;
+                s_tr[(3 * tid + k) * TSW + j * NV + 2 * h + 1] = s2.y;
+            }
+    __syncthreads();   // s_side ready
+
+    for (int hh = tid; hh < H; hh += kTile) {
+        if (hh != tid) {
+            hw = __ldg(a.halo_list + h0 + hh);
+            const int ne = hw >> 2;
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+                for (int i = 0; i < NP; ++i)
+                    cn2[h][i] = mk2(__ldg(u + ((2 * h) * NP + i) * SE + ne),
+                                            __ldg(u + ((2 * h + 1) * NP + i) * SE + ne));
+        }
+        const R *ts = s_side + (hw & 3) * NP * NQ1;
+        R2 tr2[NQ1][2];
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) tr2[j][h] = mk2(R(0), R(0));
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+#pragma unroll
+            for (int j = 0; j < NQ1; ++j) {
+                const R2 t2 = dup2(ts[i * NQ1 + j]);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) tr2[j][h] = fma2(cn2[h][i], t2, tr2[j][h]);
+            }
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                s_tr[(3 * kTile + hh) * TSW + j * NV + 2 * h] = tr2[j][h].x;
+                s_tr[(3 * kTile + hh) * TSW + j * NV + 2 * h + 1] = tr2[j][h].y;
+            }
+    }
+
+    R2 rhs2[2][NP];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int i = 0; i < NP; ++i) rhs2[h][i] = mk2(R(0), R(0));
+
+    R invJ = R(0), xr = R(0), yr = R(0), xs = R(0), ys = R(0);
+    if (live) {
+        const R *__restrict__ geo = static_cast<const R *>(a.geo);
+        invJ = __ldg(geo + e);
+        xr = __ldg(geo + SE + e);
+        yr = __ldg(geo + 2 * SE + e);
+        xs = __ldg(geo + 3 * SE + e);
+        ys = __ldg(geo + 4 * SE + e);
+#if DGX_ROLLED_VOLUME
+#pragma unroll 1
+#else
+#pragma unroll
+#endif
+        for (int q = 0; q < NQ; ++q) {
+            R2 U2[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                R2 s2 = mk2(R(0), R(0));
+#pragma unroll
+                for (int i = 0; i < NP; ++i) s2 = fma2(c2[h][i], dup2(c_tab[L::PHI + i * NQ + q]), s2);
+                U2[h] = s2;
+            }
+            const R U[4] = {U2[0].x, U2[0].y, U2[1].x, U2[1].y};
+            R fx[NV], fy[NV];
+            phys_flux<EQ>(U, g, ax, ay, fx, fy);
+            R hr[NV], hs[NV];
+#pragma unroll
+            for (int n = 0; n < NV; ++n) {
+                hr[n] = fx[n] * ys - fy[n] * xs;
+                hs[n] = fy[n] * xr - fx[n] * yr;
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const R2 hr2 = mk2(hr[2 * h], hr[2 * h + 1]);
+                const R2 hs2 = mk2(hs[2 * h], hs[2 * h + 1]);
+#pragma unroll
+                for (int i = 0; i < NP; ++i)
+                    rhs2[h][i] = fma2(dup2(c_tab[L::GX + i * NQ + q]), hr2,
+                                      fma2(dup2(c_tab[L::GY + i * NQ + q]), hs2, rhs2[h][i]));
+            }
+        }
+    }
+    __syncthreads();   // all traces of the tile and its halo are in shared memory
+    if (!live) return pre;
+
+#if DGX_ROLLED_SIDES
+#pragma unroll 1
+#else
+#pragma unroll
+#endif
+    for (int k = 0; k < 3; ++k) {
+        const int word = pick3(sw[0], sw[1], sw[2], k);
+        const R nx = pick3(snx[0], snx[1], snx[2], k), ny = pick3(sny[0], sny[1], sny[2], k);
+        const R hl = pick3(shl[0], shl[1], shl[2], k);
+        const int own = 3 * tid + k;
+        const bool bnd = BND && word < 0;
+        const int slot = bnd ? own : (word >> 1);
+        const int il = bnd ? 1 : (word & 1);
+        const R *s_own = s_tr + own * TSW;
+        const R *s_nbr = s_tr + slot * TSW;
+        R2 Fh2[NQ1][2];
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j) {
+            R UO[NV], UN[NV], UL[NV], UR[NV], Fh[NV];
+#pragma unroll
+            for (int n = 0; n < NV; ++n) {
+                UO[n] = s_own[j * NV + n];
+                UN[n] = s_nbr[(NQ1 - 1 - j) * NV + n];
+            }
+            if constexpr (BND) {
+                if (bnd) boundary_ghost<P, EQ>(a, word, k, j, e, UO, nx, ny, UN);
+            }
+#pragma unroll
+            for (int n = 0; n < NV; ++n) {
+                UL[n] = il ? UO[n] : UN[n];
+                UR[n] = il ? UN[n] : UO[n];
+            }
+            num_flux<EQ>(UL, UR, nx, ny, llf, g, ax, ay, Fh);
+            Fh2[j][0] = mk2(Fh[0], Fh[1]);
+            Fh2[j][1] = mk2(Fh[2], Fh[3]);
+        }
+        const R2 sg2 = dup2(il ? -hl : hl);
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int i = 0; i < NP; ++i) {
+                R2 s2 = mk2(R(0), R(0));
+#pragma unroll
+                for (int j = 0; j < NQ1; ++j) s2 = fma2(dup2(c_tab[L::LIFT + (k * NP + i) * NQ1 + j]), Fh2[j][h], s2);
+                rhs2[h][i] = fma2(sg2, s2, rhs2[h][i]);
+            }
+    }
+
+    R rhs[NV][NP], c[NV][NP];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+            rhs[2 * h][i] = rhs2[h][i].x;
+            rhs[2 * h + 1][i] = rhs2[h][i].y;
+            c[2 * h][i] = c2[h][i].x;
+            c[2 * h + 1][i] = c2[h][i].y;
+        }
+    return stage_epilogue<P, EQ>(a, rhs, c, dt, invJ, e, SE, pre, s_pre, bar, parity, tid);
+}
+
 template <int P, int EQ, bool BND>
 __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, unsigned char *smem_raw,
                                            const unsigned parity) {
+    if constexpr (DGX_PAIRED && sizeof(R) == 4 && EQ == DGX_EULER) {
+        return stage_tile_pair<P, BND>(a, tile, smem_raw, parity);
+    }
     using L = Lay<P>;
     constexpr int NP = L::NP, NQ = L::NQ, NQ1 = L::NQ1;
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
