@@ -476,8 +476,34 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 __device__ __forceinline__ double2 fma2(double2 a, double2 b, double2 c) {
     return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
 }
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ double2 fmul2(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ double2 fadd2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ R2 mk2(R x, R y) { R2 v; v.x = x; v.y = y; return v; }
 __device__ __forceinline__ R2 dup2(R t) { return mk2(t, t); }
+
+// The Euler LLF flux of num_flux with the left and right states as the lanes
+// of pairs: Ulr[n] = (UL[n], UR[n]).  Both elements of a side call it with the
+// same arguments and get the same bits.
+__device__ __forceinline__ void num_flux_euler_pair(const R2 (&Ulr)[4], R nx, R ny, int llf, R g, R *Fh) {
+    const R2 ir = mk2(rrcp(Ulr[0].x), rrcp(Ulr[0].y));
+    const R2 u = fmul2(Ulr[1], ir), v = fmul2(Ulr[2], ir);
+    const R2 kin = fma2(Ulr[2], v, fmul2(Ulr[1], u));
+    const R2 p = fmul2(dup2(g - R(1)), fma2(dup2(R(-0.5)), kin, Ulr[3]));
+    const R2 nx2 = dup2(nx), ny2 = dup2(ny);
+    const R2 un = fma2(u, nx2, fmul2(v, ny2));
+    R lam = R(0);
+    if (llf) {
+        const R2 c2 = fmul2(fmul2(dup2(g), p), ir);
+        const R ll = fabs(un.x) + rsqrt_(c2.x), lr = fabs(un.y) + rsqrt_(c2.y);
+        lam = ll > lr ? ll : lr;
+    }
+    const R2 f[4] = {fma2(Ulr[1], nx2, fmul2(Ulr[2], ny2)), fma2(Ulr[1], un, fmul2(p, nx2)),
+                     fma2(Ulr[2], un, fmul2(p, ny2)), fmul2(fadd2(Ulr[3], p), un)};
+#pragma unroll
+    for (int n = 0; n < 4; ++n) Fh[n] = R(0.5) * ((f[n].x + f[n].y) + lam * (Ulr[n].x - Ulr[n].y));
+}
 
 // FP32 Euler: stage_tile with the four variables held as the pairs
 // (rho, rho u) and (rho v, E), so that every basis contraction (traces, point
@@ -619,6 +645,7 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
         yr = __ldg(geo + 2 * SE + e);
         xs = __ldg(geo + 3 * SE + e);
         ys = __ldg(geo + 4 * SE + e);
+        const R2 ys2 = dup2(ys), xr2 = dup2(xr), nxs2 = dup2(-xs), nyr2 = dup2(-yr);
 #if DGX_ROLLED_VOLUME
 #pragma unroll 1
 #else
@@ -636,16 +663,12 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
             const R U[4] = {U2[0].x, U2[0].y, U2[1].x, U2[1].y};
             R fx[NV], fy[NV];
             phys_flux<EQ>(U, g, ax, ay, fx, fy);
-            R hr[NV], hs[NV];
-#pragma unroll
-            for (int n = 0; n < NV; ++n) {
-                hr[n] = fx[n] * ys - fy[n] * xs;
-                hs[n] = fy[n] * xr - fx[n] * yr;
-            }
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const R2 hr2 = mk2(hr[2 * h], hr[2 * h + 1]);
-                const R2 hs2 = mk2(hs[2 * h], hs[2 * h + 1]);
+                // (fx ys - fy xs, fy xr - fx yr) of the pair's two variables
+                const R2 fx2 = mk2(fx[2 * h], fx[2 * h + 1]), fy2 = mk2(fy[2 * h], fy[2 * h + 1]);
+                const R2 hr2 = fma2(fx2, ys2, fmul2(fy2, nxs2));
+                const R2 hs2 = fma2(fy2, xr2, fmul2(fx2, nyr2));
 #pragma unroll
                 for (int i = 0; i < NP; ++i)
                     rhs2[h][i] = fma2(dup2(c_tab[L::GX + i * NQ + q]), hr2,
@@ -674,7 +697,8 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
         R2 Fh2[NQ1][2];
 #pragma unroll
         for (int j = 0; j < NQ1; ++j) {
-            R UO[NV], UN[NV], UL[NV], UR[NV], Fh[NV];
+            R UO[NV], UN[NV], Fh[NV];
+            R2 Ulr[NV];
 #pragma unroll
             for (int n = 0; n < NV; ++n) {
                 UO[n] = s_own[j * NV + n];
@@ -684,11 +708,8 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
                 if (bnd) boundary_ghost<P, EQ>(a, word, k, j, e, UO, nx, ny, UN);
             }
 #pragma unroll
-            for (int n = 0; n < NV; ++n) {
-                UL[n] = il ? UO[n] : UN[n];
-                UR[n] = il ? UN[n] : UO[n];
-            }
-            num_flux<EQ>(UL, UR, nx, ny, llf, g, ax, ay, Fh);
+            for (int n = 0; n < NV; ++n) Ulr[n] = il ? mk2(UO[n], UN[n]) : mk2(UN[n], UO[n]);
+            num_flux_euler_pair(Ulr, nx, ny, llf, g, Fh);
             Fh2[j][0] = mk2(Fh[0], Fh[1]);
             Fh2[j][1] = mk2(Fh[2], Fh[3]);
         }
