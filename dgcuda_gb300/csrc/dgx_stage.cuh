@@ -49,12 +49,12 @@
 #define DGX_ROLLED_SIDES 0
 #endif
 #ifndef DGX_ROLLED_TRACES
-#define DGX_ROLLED_TRACES 1
+#define DGX_ROLLED_TRACES 0
 #endif
 
 namespace dgx {
 
-static __constant__ DGX_REAL c_tab[kTableTotal];
+static __constant__ __align__(16) DGX_REAL c_tab[kTableTotal];
 constexpr bool kStageBnd = DGX_STAGE_BND != 0;
 
 template <typename T>
@@ -646,33 +646,74 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
         xs = __ldg(geo + 3 * SE + e);
         ys = __ldg(geo + 4 * SE + e);
         const R2 ys2 = dup2(ys), xr2 = dup2(xr), nxs2 = dup2(-xs), nyr2 = dup2(-yr);
-#if DGX_ROLLED_VOLUME
-#pragma unroll 1
-#else
-#pragma unroll
-#endif
-        for (int q = 0; q < NQ; ++q) {
-            R2 U2[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                R2 s2 = mk2(R(0), R(0));
-#pragma unroll
-                for (int i = 0; i < NP; ++i) s2 = fma2(c2[h][i], dup2(c_tab[L::PHI + i * NQ + q]), s2);
-                U2[h] = s2;
-            }
+        // point values of the pair h at the point whose table values t(i) gives
+        // metric terms (fx ys - fy xs, fy xr - fx yr) per variable pair
+        auto metric = [&](const R2 (&U2)[2], R2 (&hr2)[2], R2 (&hs2)[2]) {
             const R U[4] = {U2[0].x, U2[0].y, U2[1].x, U2[1].y};
             R fx[NV], fy[NV];
             phys_flux<EQ>(U, g, ax, ay, fx, fy);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                // (fx ys - fy xs, fy xr - fx yr) of the pair's two variables
                 const R2 fx2 = mk2(fx[2 * h], fx[2 * h + 1]), fy2 = mk2(fy[2 * h], fy[2 * h + 1]);
-                const R2 hr2 = fma2(fx2, ys2, fmul2(fy2, nxs2));
-                const R2 hs2 = fma2(fy2, xr2, fmul2(fx2, nyr2));
+                hr2[h] = fma2(fx2, ys2, fmul2(fy2, nxs2));
+                hs2[h] = fma2(fy2, xr2, fmul2(fx2, nyr2));
+            }
+        };
+        if constexpr (NQ % 2 == 0 && L::PHI % 2 == 0 && (NP * NQ) % 2 == 0) {
+            // two points per iteration: the tables of points q, q+1 are adjacent,
+            // one 2-value constant load serves both
+#pragma unroll 1
+            for (int q = 0; q < NQ; q += 2) {
+                R2 Ua[2], Ub[2];
 #pragma unroll
-                for (int i = 0; i < NP; ++i)
-                    rhs2[h][i] = fma2(dup2(c_tab[L::GX + i * NQ + q]), hr2,
-                                      fma2(dup2(c_tab[L::GY + i * NQ + q]), hs2, rhs2[h][i]));
+                for (int h = 0; h < 2; ++h) {
+                    R2 sa = mk2(R(0), R(0)), sb = mk2(R(0), R(0));
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) {
+                        const R2 t = *reinterpret_cast<const R2 *>(&c_tab[L::PHI + i * NQ + q]);
+                        sa = fma2(c2[h][i], dup2(t.x), sa);
+                        sb = fma2(c2[h][i], dup2(t.y), sb);
+                    }
+                    Ua[h] = sa;
+                    Ub[h] = sb;
+                }
+                R2 hra[2], hsa[2], hrb[2], hsb[2];
+                metric(Ua, hra, hsa);
+                metric(Ub, hrb, hsb);
+#pragma unroll
+                for (int i = 0; i < NP; ++i) {
+                    const R2 tx = *reinterpret_cast<const R2 *>(&c_tab[L::GX + i * NQ + q]);
+                    const R2 ty = *reinterpret_cast<const R2 *>(&c_tab[L::GY + i * NQ + q]);
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        rhs2[h][i] = fma2(dup2(tx.x), hra[h], fma2(dup2(ty.x), hsa[h], rhs2[h][i]));
+                        rhs2[h][i] = fma2(dup2(tx.y), hrb[h], fma2(dup2(ty.y), hsb[h], rhs2[h][i]));
+                    }
+                }
+            }
+        } else {
+#if DGX_ROLLED_VOLUME
+#pragma unroll 1
+#else
+#pragma unroll
+#endif
+            for (int q = 0; q < NQ; ++q) {
+                R2 U2[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    R2 s2 = mk2(R(0), R(0));
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) s2 = fma2(c2[h][i], dup2(c_tab[L::PHI + i * NQ + q]), s2);
+                    U2[h] = s2;
+                }
+                R2 hr2[2], hs2[2];
+                metric(U2, hr2, hs2);
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int i = 0; i < NP; ++i)
+                        rhs2[h][i] = fma2(dup2(c_tab[L::GX + i * NQ + q]), hr2[h],
+                                          fma2(dup2(c_tab[L::GY + i * NQ + q]), hs2[h], rhs2[h][i]));
             }
         }
     }

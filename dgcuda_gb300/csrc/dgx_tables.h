@@ -26,8 +26,9 @@ DGX_HD constexpr int num_quad1(int p) { return p + 1; }
 // Per-order block of the device tables: phi[np*nq], gx[np*nq], gy[np*nq],
 // side[3*np*nq1], lift[3*np*nq1] (= w1[j] * side), w1[nq1], and the reference
 // coordinates of the side points srs[3][nq1][2].
-DGX_HD constexpr int table_block(int p) {
-    return 3 * num_modes(p) * num_quad(p) + 6 * num_modes(p) * num_quad1(p) + num_quad1(p) + 6 * num_quad1(p);
+DGX_HD constexpr int table_block(int p) {   // rounded up to 4 values: every order's block starts 16-byte aligned
+    return (3 * num_modes(p) * num_quad(p) + 6 * num_modes(p) * num_quad1(p) + num_quad1(p) + 6 * num_quad1(p) + 3) &
+           ~3;
 }
 DGX_HD constexpr int table_offset(int p) { return p == 0 ? 0 : table_offset(p - 1) + table_block(p - 1); }
 constexpr int kTableTotal = table_offset(kMaxOrder + 1);
