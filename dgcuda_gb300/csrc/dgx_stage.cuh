@@ -55,6 +55,26 @@
 namespace dgx {
 
 static __constant__ __align__(16) DGX_REAL c_tab[kTableTotal];
+
+// The same tables transposed, mode index fastest and padded to an even count
+// (the pad is 0): phi, gx, gy as [q][i], side and lift as [side][j][i].  Modes
+// 2m and 2m+1 are adjacent and 8-byte aligned, the operand of one paired FMA.
+DGX_HD constexpr int np_even(int p) { return (num_modes(p) + 1) & ~1; }
+DGX_HD constexpr int tabt_block(int p) { return ((3 * num_quad(p) + 6 * num_quad1(p)) * np_even(p) + 3) & ~3; }
+DGX_HD constexpr int tabt_offset(int p) { return p == 0 ? 0 : tabt_offset(p - 1) + tabt_block(p - 1); }
+constexpr int kTabTTotal = tabt_offset(kMaxOrder + 1);
+template <int P>
+struct LayT {
+    static constexpr int NPP = np_even(P), NQ = num_quad(P), NQ1 = num_quad1(P);
+    static constexpr int PHI = tabt_offset(P);
+    static constexpr int GX = PHI + NQ * NPP;
+    static constexpr int GY = GX + NQ * NPP;
+    static constexpr int SIDE = GY + NQ * NPP;
+    static constexpr int LIFT = SIDE + 3 * NQ1 * NPP;
+};
+#ifdef DGX_REAL_F32
+static __constant__ __align__(16) float c_tabT[kTabTTotal];
+#endif
 constexpr bool kStageBnd = DGX_STAGE_BND != 0;
 
 template <typename T>
@@ -277,7 +297,7 @@ __device__ __noinline__ void boundary_ghost(const StageArgs &a, int tag, int k, 
 // so a thread addresses a whole slot from one base register and threads
 // reading their own slots 3*tid + k (stride 3*TSW, odd) hit distinct banks.
 template <int P, int NV>
-DGX_HD constexpr int side_table_words() { return (3 * num_modes(P) * num_quad1(P) + 3) & ~3; }
+DGX_HD constexpr int side_table_words() { return (3 * ((num_modes(P) + 1) & ~1) * num_quad1(P) + 3) & ~3; }
 template <int P, int NV>
 DGX_HD constexpr int slot_words() { return (NV * num_quad1(P)) | 1; }
 
@@ -779,12 +799,197 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
     return stage_epilogue<P, EQ>(a, rhs, c, dt, invJ, e, SE, pre, s_pre, bar, parity, tid);
 }
 
+#ifdef DGX_REAL_F32
+// FP32 advection: stage_tile with the modes held in pairs (2m, 2m+1) and the
+// transposed tables, so that every basis contraction issues one paired FMA per
+// two modes.  Sums over modes (traces, point values) run as two partial sums,
+// even and odd modes, added at the end; sums into a mode (volume projection,
+// lift) keep the scalar kernel's operands and order.  An odd mode count is
+// padded with a zero mode.
+template <int P, bool BND>
+__device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const int tile, unsigned char *smem_raw,
+                                                    const unsigned parity) {
+    using L = Lay<P>;
+    using T = LayT<P>;
+    constexpr int NP = L::NP, NQ = L::NQ, NQ1 = L::NQ1, NPP = T::NPP, NH = NPP / 2;
+    constexpr int EQ = DGX_ADVECTION, NV = 1;
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem_raw);
+    float *s_side = reinterpret_cast<float *>(smem_raw + 16);   // [side][j][i], rows of NPP
+    float *s_tr = s_side + side_table_words<P, NV>();
+    const int nslot = a.nslot;
+    constexpr int TSW = slot_words<P, NV>();
+    float *s_pre = s_tr + static_cast<size_t>(TSW) * nslot;
+
+    float dt;
+    if (a.mode == 0) {
+        dt = float(a.dt);
+    } else {
+        dt = float(a.scal[0]);
+        if (dt == 0.0f) return false;   // the run has reached its end time (uniform over the CTA)
+    }
+    const int E = a.E;
+    const int tid = threadIdx.x;
+    const int e = tile * kTile + tid;
+    const bool live = e < E;
+    const size_t SE = static_cast<size_t>(E);
+    const float ax = a.axf, ay = a.ayf;
+    const int llf = a.flux == DGX_FLUX_LLF;
+    const float *__restrict__ u = static_cast<const float *>(a.u);
+    auto t2 = [](int off) { return *reinterpret_cast<const float2 *>(&c_tabT[off]); };
+
+    for (int t = tid; t < 3 * NQ1 * NPP; t += kTile) s_side[t] = c_tabT[T::SIDE + t];
+    const bool pre = issue_prefetch<P, NV>(a, tile, bar, s_pre, tid);
+
+    float2 c2[NH];
+#pragma unroll
+    for (int m = 0; m < NH; ++m) {
+        const float lo = live ? __ldg(u + (2 * m) * SE + e) : 0.0f;
+        const float hi = (live && 2 * m + 1 < NP) ? __ldg(u + (2 * m + 1) * SE + e) : 0.0f;
+        c2[m] = make_float2(lo, hi);
+    }
+
+    int sw[3];
+    float snx[3], sny[3], shl[3];
+    {
+        const int *__restrict__ nbr = a.nbr;
+        const float *__restrict__ fn = static_cast<const float *>(a.fn);
+        const int ee = live ? e : 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            sw[k] = __ldg(nbr + k * SE + ee);
+            snx[k] = __ldg(fn + (3 * k + 0) * SE + ee);
+            sny[k] = __ldg(fn + (3 * k + 1) * SE + ee);
+            shl[k] = __ldg(fn + (3 * k + 2) * SE + ee);
+        }
+    }
+
+    const int h0 = __ldg(a.halo_off + tile), H = __ldg(a.halo_off + tile + 1) - h0;
+    float2 cn2[NH];
+    int hw = tid < H ? __ldg(a.halo_list + h0 + tid) : -1;
+    auto gather = [&](int ne) {
+#pragma unroll
+        for (int m = 0; m < NH; ++m)
+            cn2[m] = make_float2(__ldg(u + (2 * m) * SE + ne), 2 * m + 1 < NP ? __ldg(u + (2 * m + 1) * SE + ne) : 0.0f);
+    };
+    if (hw >= 0) gather(hw >> 2);
+
+    // own traces on the three sides
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j) {
+            float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int m = 0; m < NH; ++m) acc = fma2(c2[m], t2(T::SIDE + (k * NQ1 + j) * NPP + 2 * m), acc);
+            s_tr[(3 * tid + k) * TSW + j] = acc.x + acc.y;
+        }
+    __syncthreads();   // s_side ready
+
+    for (int hh = tid; hh < H; hh += kTile) {
+        if (hh != tid) {
+            hw = __ldg(a.halo_list + h0 + hh);
+            gather(hw >> 2);
+        }
+        const float *ts = s_side + (hw & 3) * NQ1 * NPP;
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j) {
+            float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int m = 0; m < NH; ++m)
+                acc = fma2(cn2[m], *reinterpret_cast<const float2 *>(ts + j * NPP + 2 * m), acc);
+            s_tr[(3 * kTile + hh) * TSW + j] = acc.x + acc.y;
+        }
+    }
+
+    float2 rhs2[NH];
+#pragma unroll
+    for (int m = 0; m < NH; ++m) rhs2[m] = make_float2(0.0f, 0.0f);
+
+    float invJ = 0.0f;
+    if (live) {
+        const float *__restrict__ geo = static_cast<const float *>(a.geo);
+        invJ = __ldg(geo + e);
+        const float xr = __ldg(geo + SE + e), yr = __ldg(geo + 2 * SE + e);
+        const float xs = __ldg(geo + 3 * SE + e), ys = __ldg(geo + 4 * SE + e);
+#if DGX_ROLLED_VOLUME
+#pragma unroll 1
+#else
+#pragma unroll
+#endif
+        for (int q = 0; q < NQ; ++q) {
+            float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int m = 0; m < NH; ++m) acc = fma2(c2[m], t2(T::PHI + q * NPP + 2 * m), acc);
+            const float U[1] = {acc.x + acc.y};
+            float fx[1], fy[1];
+            phys_flux<EQ>(U, a.gammaf, ax, ay, fx, fy);
+            const float2 hr = dup2(fx[0] * ys - fy[0] * xs), hs = dup2(fy[0] * xr - fx[0] * yr);
+#pragma unroll
+            for (int m = 0; m < NH; ++m)
+                rhs2[m] = fma2(t2(T::GX + q * NPP + 2 * m), hr, fma2(t2(T::GY + q * NPP + 2 * m), hs, rhs2[m]));
+        }
+    }
+    __syncthreads();   // all traces of the tile and its halo are in shared memory
+    if (!live) return pre;
+
+#if DGX_ROLLED_SIDES
+#pragma unroll 1
+#else
+#pragma unroll
+#endif
+    for (int k = 0; k < 3; ++k) {
+        const int word = pick3(sw[0], sw[1], sw[2], k);
+        const float nx = pick3(snx[0], snx[1], snx[2], k), ny = pick3(sny[0], sny[1], sny[2], k);
+        const float hl = pick3(shl[0], shl[1], shl[2], k);
+        const int own = 3 * tid + k;
+        const bool bnd = BND && word < 0;
+        const int slot = bnd ? own : (word >> 1);
+        const int il = bnd ? 1 : (word & 1);
+        const float *s_own = s_tr + own * TSW;
+        const float *s_nbr = s_tr + slot * TSW;
+        float2 Fh2[NQ1];
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j) {
+            float UO[1] = {s_own[j]}, UN[1] = {s_nbr[NQ1 - 1 - j]};
+            if constexpr (BND) {
+                if (bnd) boundary_ghost<P, EQ>(a, word, k, j, e, UO, nx, ny, UN);
+            }
+            const float UL[1] = {il ? UO[0] : UN[0]}, UR[1] = {il ? UN[0] : UO[0]};
+            float Fh[1];
+            num_flux<EQ>(UL, UR, nx, ny, llf, a.gammaf, ax, ay, Fh);
+            Fh2[j] = dup2(Fh[0]);
+        }
+        const float2 sg2 = dup2(il ? -hl : hl);
+#pragma unroll
+        for (int m = 0; m < NH; ++m) {
+            float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int j = 0; j < NQ1; ++j) acc = fma2(t2(T::LIFT + (k * NQ1 + j) * NPP + 2 * m), Fh2[j], acc);
+            rhs2[m] = fma2(sg2, acc, rhs2[m]);
+        }
+    }
+
+    float rhs[1][NP], c[1][NP];
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        rhs[0][i] = (i & 1) ? rhs2[i / 2].y : rhs2[i / 2].x;
+        c[0][i] = (i & 1) ? c2[i / 2].y : c2[i / 2].x;
+    }
+    return stage_epilogue<P, EQ>(a, rhs, c, dt, invJ, e, SE, pre, s_pre, bar, parity, tid);
+}
+#endif
+
 template <int P, int EQ, bool BND>
 __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, unsigned char *smem_raw,
                                            const unsigned parity) {
     if constexpr (DGX_PAIRED && sizeof(R) == 4 && EQ == DGX_EULER) {
         return stage_tile_pair<P, BND>(a, tile, smem_raw, parity);
     }
+#ifdef DGX_REAL_F32
+    if constexpr (DGX_PAIRED && EQ == DGX_ADVECTION) {
+        return stage_tile_adv_pair<P, BND>(a, tile, smem_raw, parity);
+    }
+#endif
     using L = Lay<P>;
     constexpr int NP = L::NP, NQ = L::NQ, NQ1 = L::NQ1;
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
@@ -1179,6 +1384,31 @@ static int upload_tables_impl() {
         }
     }
     DGX_TRY_CUDA(cudaMemcpyToSymbol(c_tab, host, sizeof(host)));
+#ifdef DGX_REAL_F32
+    static float ht[kTabTTotal];
+    for (int p = 0; p <= kMaxOrder; ++p) {
+        const Tables &T = tables(p);
+        const int np = T.np, nq = T.nq, nq1 = T.nq1, npp = np_even(p);
+        float *b = ht + tabt_offset(p);
+        for (int q = 0; q < nq; ++q)
+            for (int i = 0; i < npp; ++i) {
+                const bool m = i < np;
+                b[q * npp + i] = m ? static_cast<float>(T.phi[i * nq + q]) : 0.0f;
+                b[(nq + q) * npp + i] = m ? static_cast<float>(T.gx[i * nq + q]) : 0.0f;
+                b[(2 * nq + q) * npp + i] = m ? static_cast<float>(T.gy[i * nq + q]) : 0.0f;
+            }
+        float *sd = b + 3 * nq * npp, *lf = sd + 3 * nq1 * npp;
+        for (int k = 0; k < 3; ++k)
+            for (int j = 0; j < nq1; ++j)
+                for (int i = 0; i < npp; ++i) {
+                    const int o = (k * np + i) * nq1 + j;
+                    const bool m = i < np;
+                    sd[(k * nq1 + j) * npp + i] = m ? static_cast<float>(T.side[o]) : 0.0f;
+                    lf[(k * nq1 + j) * npp + i] = m ? static_cast<float>(T.w1[j] * T.side[o]) : 0.0f;
+                }
+    }
+    DGX_TRY_CUDA(cudaMemcpyToSymbol(c_tabT, ht, sizeof(ht)));
+#endif
     return DGX_OK;
 }
 

@@ -1,6 +1,7 @@
 // FP32 instantiation of the fused stage kernel (the plain FP32 path),
 // for meshes without boundary sides.
 #define DGX_REAL float
+#define DGX_REAL_F32
 #define DGX_STAGE_BND 0
 #include "dgx_stage.cuh"
 
