@@ -911,11 +911,9 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
         invJ = __ldg(geo + e);
         const float xr = __ldg(geo + SE + e), yr = __ldg(geo + 2 * SE + e);
         const float xs = __ldg(geo + 3 * SE + e), ys = __ldg(geo + 4 * SE + e);
-#if DGX_ROLLED_VOLUME
-#pragma unroll 1
-#else
-#pragma unroll
-#endif
+        // p = 4 unrolled (measured 8 % faster), the lower orders rolled (p = 3
+        // unrolled was 10 % slower)
+#pragma unroll(P == 4 ? NQ : 1)
         for (int q = 0; q < NQ; ++q) {
             float2 acc = make_float2(0.0f, 0.0f);
 #pragma unroll
@@ -1212,6 +1210,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
 #ifndef DGX_MIN_CTAS_P3
 #define DGX_MIN_CTAS_P3 3
 #endif
+
 template <int P>
 constexpr int min_ctas() { return P <= 3 ? DGX_MIN_CTAS_P3 : 2; }
 
