@@ -57,7 +57,8 @@ class ServerStats(C.Structure):
                 ("p99_latency_s", C.c_double), ("max_latency_s", C.c_double),
                 ("device_bytes_in_use", C.c_size_t), ("admit_seconds", C.c_double),
                 ("repack_seconds", C.c_double), ("retire_seconds", C.c_double),
-                ("idle_seconds", C.c_double)]
+                ("idle_seconds", C.c_double), ("pool_hits", C.c_longlong),
+                ("pool_misses", C.c_longlong), ("cached_meshes", C.c_longlong)]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = 0, 1, 2, 3, 4

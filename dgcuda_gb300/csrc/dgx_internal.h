@@ -99,8 +99,14 @@ public:
     void put(void *p, size_t bytes);
     void trim();                                   // free the cached blocks not carved from slabs
     size_t cached_bytes();
-    long long hits() const { return hits_; }
-    long long misses() const { return misses_; }
+    long long hits() {
+        std::lock_guard<std::mutex> lk(mu_);
+        return hits_;
+    }
+    long long misses() {
+        std::lock_guard<std::mutex> lk(mu_);
+        return misses_;
+    }
     // 4 KiB .. 64 KiB: powers of two; above: 8 classes per octave
     static size_t size_class(size_t bytes);
 private:

@@ -624,6 +624,9 @@ int dgx_server_get_stats(dgx_server *s, dgx_server_stats *out) {
     out->repack_seconds = s->repack_s;
     out->retire_seconds = s->retire_s;
     out->idle_seconds = s->idle_s;
+    out->pool_hits = s->pool->hits();
+    out->pool_misses = s->pool->misses();
+    out->cached_meshes = static_cast<long long>(s->meshes.size());
     out->repacks = s->repacks;
     out->steps = s->steps;
     out->device_bytes_in_use = s->in_use + s->mesh_bytes;

@@ -374,6 +374,9 @@ typedef struct dgx_server_stats {
     double repack_seconds;       /* worker time spent rebuilding the batch              */
     double retire_seconds;       /* worker time spent reading out and freeing finished solves */
     double idle_seconds;         /* worker time spent waiting for requests              */
+    long long pool_hits;         /* mesh and solver blocks reused from the server's pool */
+    long long pool_misses;       /* blocks the pool had to allocate                     */
+    long long cached_meshes;     /* meshes in the cache (running and idle)              */
 } dgx_server_stats;
 /* budget_bytes: admission limit on the estimated device footprint of running
  * requests; max_active: slot limit. */

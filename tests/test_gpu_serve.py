@@ -67,9 +67,37 @@ def test_budget_admission_serialises_but_completes(gpu):
     srv = Server(budget_bytes=64 << 10, max_active=64)
     ids = [srv.submit(request(**dict(sp, seed=sp["seed"] + i))) for i in range(4)]
     assert srv.wait_idle(120.0) == _ffi.OK
-    assert srv.stats()["completed"] == 4
+    st = srv.stats()
+    assert st["completed"] == 4
+    # each admission had to evict the previous request's idle mesh to fit
+    assert st["cached_meshes"] == 1
     for rid in ids:
         assert srv.status(rid)[0] == _ffi.REQ_DONE
+    srv.close()
+
+
+def test_pool_reuse_and_mesh_cache(gpu):
+    sp = specs()
+    srv = Server(budget_bytes=1 << 30, max_active=64)
+    first = [srv.submit(request(**dict(s, keep_state=1))) for s in sp]
+    assert srv.wait_idle(120.0) == _ffi.OK
+    st1 = srv.stats()
+    assert st1["completed"] == len(sp) and st1["pool_misses"] > 0
+    assert st1["cached_meshes"] == len({(s["n"], s["lx"], s["seed"]) for s in sp})
+    # the same requests again: their meshes come from the cache, their solver
+    # blocks from the pool (nothing is allocated), and the results repeat
+    second = [srv.submit(request(**dict(s, keep_state=1))) for s in sp]
+    assert srv.wait_idle(120.0) == _ffi.OK
+    st2 = srv.stats()
+    assert st2["completed"] == 2 * len(sp)
+    assert st2["pool_misses"] == st1["pool_misses"] and st2["pool_hits"] >= st1["pool_hits"] + len(sp)
+    assert st2["cached_meshes"] == st1["cached_meshes"]
+    for s, a, b in zip(sp, first, second):
+        size = (4 if s["equation"] == _ffi.EULER else 1) * (s["order"] + 1) * (s["order"] + 2) // 2 * 2 * s["n"] ** 2
+        ra, rb = srv.result(a, size), srv.result(b, size)
+        np.testing.assert_array_equal(ra[0], rb[0])
+        np.testing.assert_array_equal(ra[1], rb[1])
+        assert ra[2] == rb[2] and ra[3] == rb[3]
     srv.close()
 
 
