@@ -415,7 +415,10 @@ def run_served(rates=(50, 200, 1000, 2000, 0), count: int = 400):
         out.append({"rate_req_s": rate if rate > 0 else "all at once", "requests": count, "completed": st["completed"],
                     "failed": st["failed"], "p50_s": st["p50_latency_s"],
                     "p99_s": st["p99_latency_s"], "dof_updates": st["dof_updates"],
-                    "value": st["dof_updates"] / wall, "wall_s": wall, "repacks": st["repacks"]})
+                    "value": st["dof_updates"] / wall, "wall_s": wall, "repacks": st["repacks"],
+                    "worker_s": {"admit": st["admit_seconds"], "repack": st["repack_seconds"],
+                                 "step": st["busy_seconds"], "retire": st["retire_seconds"],
+                                 "idle": st["idle_seconds"]}})
         if plain is None:
             # the same requests one by one on the plain path
             import torch

@@ -58,7 +58,8 @@ struct dgx_batch {
     const unsigned int **d_status = nullptr;
     const long long **d_steps = nullptr;
     double *d_progress = nullptr;          // [n][4]: t, dt, status, steps
-    double *h_progress = nullptr;          // pinned copy
+    std::vector<double> h_progress;        // host copy
+    DeviceBlock block;                     // every device array of the batch, one allocation
     std::vector<BatchClass> classes;
     DtArgs *d_dt = nullptr;
     int2 *d_cfl_items = nullptr;
@@ -90,43 +91,57 @@ int class_launch(dgx_batch *b, BatchClass &k, int stage, cudaStream_t st) {
     return rc;
 }
 
-// Upload the per-solve stage arguments of one class for the given options.
-int class_upload(dgx_batch *b, BatchClass &k) {
-    std::vector<StageArgs> host(k.solves.size());
+// The per-solve stage arguments of one class for its options, stage-major
+// (host[stage * solves + j]); sets the class's slot count and prefetch plane,
+// and turns the prefetch off when it would not fit in shared memory.
+int class_host_args(dgx_batch *b, BatchClass &k, std::vector<StageArgs> &host) {
+    const size_t ns = k.solves.size();
+    host.resize(4 * ns);
     int nslot = 0, plane = 0;
     for (int stage = 0; stage < 4; ++stage) {
-        for (size_t j = 0; j < k.solves.size(); ++j) {
+        for (size_t j = 0; j < ns; ++j) {
             dgx_solver *sv = b->solvers[k.solves[j]];
             SolverDev &s = sv->s;
             const int saved = s.prefetch;
             s.prefetch = k.prefetch;
+            StageArgs &h = host[stage * ns + j];
             switch (stage) {
-            case 0: host[j] = make_stage_args(sv, 1, s.c, s.c, s.acc, s.ua, 0.0, 0.0); break;
-            case 1: host[j] = make_stage_args(sv, 2, s.ua, s.c, s.acc, s.ub, 0.0, 0.0); break;
-            case 2: host[j] = make_stage_args(sv, 3, s.ub, s.c, s.acc, s.ua, 0.0, 0.0); break;
-            default: host[j] = make_stage_args(sv, 4, s.ua, s.c, s.acc, s.c, 0.0, 0.0); break;
+            case 0: h = make_stage_args(sv, 1, s.c, s.c, s.acc, s.ua, 0.0, 0.0); break;
+            case 1: h = make_stage_args(sv, 2, s.ua, s.c, s.acc, s.ub, 0.0, 0.0); break;
+            case 2: h = make_stage_args(sv, 3, s.ub, s.c, s.acc, s.ua, 0.0, 0.0); break;
+            default: h = make_stage_args(sv, 4, s.ua, s.c, s.acc, s.c, 0.0, 0.0); break;
             }
             s.prefetch = saved;
-            nslot = std::max(nslot, host[j].nslot);
-            plane = std::max(plane, host[j].prefetch);
+            nslot = std::max(nslot, h.nslot);
+            plane = std::max(plane, h.prefetch);
         }
-        DGX_TRY_CUDA(cudaMemcpy(k.d_args[stage], host.data(), host.size() * sizeof(StageArgs),
-                                cudaMemcpyHostToDevice));
     }
     k.nslot = nslot;
     k.pre_plane = plane;
-    // refuse a prefetch that would not fit in shared memory
     const int pp = k.prefetch ? k.pre_plane : 0;
     const size_t smem = k.precision == DGX_FP64 ? batch_smem_f64(k.order, k.equation, nslot, pp)
                                                 : batch_smem_f32(k.order, k.equation, nslot, pp);
     if (k.prefetch && smem > 200 * 1024) {
         k.prefetch = 0;
-        return class_upload(b, k);
+        return class_host_args(b, k, host);
     }
-    // set the kernel's shared-memory limit outside any capture (grid 0: no launch)
-    BatchStageArgs probe{k.d_args[1], k.d_items, 0, 0, k.nslot, pp, k.bnd};
-    int rc = launch_batch_stage(k.precision, k.order, k.equation, probe, nullptr);
-    return rc;
+    return DGX_OK;
+}
+
+// set the class kernel's shared-memory limit outside any capture (grid 0: no launch)
+int class_configure(BatchClass &k) {
+    BatchStageArgs probe{k.d_args[1], k.d_items, 0, 0, k.nslot, k.prefetch ? k.pre_plane : 0, k.bnd};
+    return launch_batch_stage(k.precision, k.order, k.equation, probe, nullptr);
+}
+
+// Upload the per-solve stage arguments of one class for its current options
+// (the four stages' arrays are contiguous: one copy).
+int class_upload(dgx_batch *b, BatchClass &k) {
+    std::vector<StageArgs> host;
+    int rc = class_host_args(b, k, host);
+    if (rc) return rc;
+    DGX_TRY_CUDA(cudaMemcpy(k.d_args[0], host.data(), host.size() * sizeof(StageArgs), cudaMemcpyHostToDevice));
+    return class_configure(k);
 }
 
 // one step without the graph
@@ -191,20 +206,11 @@ __global__ void progress_kernel(const double *const *scal, const unsigned int *c
 
 void batch_free(dgx_batch *b) {
     destroy_graph(b);
-    if (b->d_scal) cudaFree(b->d_scal);
-    if (b->d_status) cudaFree(b->d_status);
-    if (b->d_steps) cudaFree(b->d_steps);
-    if (b->d_progress) cudaFree(b->d_progress);
-    if (b->h_progress) cudaFreeHost(b->h_progress);
+    block_free(b->block);
     for (auto &k : b->classes) {
-        for (auto p : k.d_args)
-            if (p) cudaFree(p);
-        if (k.d_items) cudaFree(k.d_items);
         if (k.stream) cudaStreamDestroy(k.stream);
         if (k.done) cudaEventDestroy(k.done);
     }
-    if (b->d_dt) cudaFree(b->d_dt);
-    if (b->d_cfl_items) cudaFree(b->d_cfl_items);
     if (b->cap) cudaStreamDestroy(b->cap);
     if (b->start) cudaEventDestroy(b->start);
     delete b;
@@ -268,6 +274,35 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
         for (int blk = 0; blk < dts[i].nblocks; ++blk) cfl_items.push_back(make_int2(i, blk));
     }
     b->n_cfl_items = static_cast<int>(cfl_items.size());
+    std::vector<std::vector<int2>> items(b->classes.size());
+    std::vector<std::vector<StageArgs>> args(b->classes.size());
+    for (size_t c = 0; c < b->classes.size() && !rc; ++c) {
+        BatchClass &k = b->classes[c];
+        for (size_t j = 0; j < k.solves.size(); ++j) {
+            const int ntiles = b->solvers[k.solves[j]]->mesh->d.num_tiles;
+            for (int t = 0; t < ntiles; ++t) items[c].push_back(make_int2(static_cast<int>(j), t));
+        }
+        k.n_items = static_cast<int>(items[c].size());
+        rc = class_host_args(b, k, args[c]);
+    }
+    if (rc) { batch_free(b); return rc; }
+    // one device block for every array of the batch, filled by one copy
+    BlockLayout L;
+    const size_t oScal = L.take<const double *>(n), oStat = L.take<const unsigned int *>(n),
+                 oSteps = L.take<const long long *>(n), oDt = L.take<DtArgs>(n), oCfl = L.take<int2>(cfl_items.size());
+    std::vector<size_t> oArgs(b->classes.size()), oItems(b->classes.size());
+    for (size_t c = 0; c < b->classes.size(); ++c) {
+        oArgs[c] = L.take<StageArgs>(args[c].size());
+        oItems[c] = L.take<int2>(items[c].size());
+    }
+    const size_t upload = L.size;
+    const size_t oProg = L.take<double>(4 * static_cast<size_t>(n));
+    rc = block_alloc(b->block, L.size, nullptr);
+    if (rc) { batch_free(b); return rc; }
+    std::vector<unsigned char> stage(upload, 0);
+    auto put = [&](size_t off, const void *src, size_t bytes) {
+        if (bytes) std::memcpy(stage.data() + off, src, bytes);
+    };
     {
         std::vector<const double *> sc(n);
         std::vector<const unsigned int *> stt(n);
@@ -277,49 +312,39 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
             stt[i] = solvers[i]->s.status;
             stp[i] = solvers[i]->s.steps;
         }
-        if (cudaMalloc(&b->d_scal, sizeof(double *) * n) != cudaSuccess ||
-            cudaMalloc(&b->d_status, sizeof(unsigned int *) * n) != cudaSuccess ||
-            cudaMalloc(&b->d_steps, sizeof(long long *) * n) != cudaSuccess ||
-            cudaMalloc(&b->d_progress, sizeof(double) * 4 * n) != cudaSuccess ||
-            cudaMallocHost(&b->h_progress, sizeof(double) * 4 * n) != cudaSuccess ||
-            cudaMemcpy(b->d_steps, stp.data(), sizeof(long long *) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(b->d_scal, sc.data(), sizeof(double *) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(b->d_status, stt.data(), sizeof(unsigned int *) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
-            set_error("batch progress buffers failed");
-            batch_free(b);
-            return DGX_ERR_NOMEM;
-        }
+        put(oScal, sc.data(), sizeof(double *) * n);
+        put(oStat, stt.data(), sizeof(unsigned int *) * n);
+        put(oSteps, stp.data(), sizeof(long long *) * n);
     }
-    if (cudaMalloc(&b->d_dt, sizeof(DtArgs) * n) != cudaSuccess ||
-        cudaMalloc(&b->d_cfl_items, sizeof(int2) * cfl_items.size()) != cudaSuccess) {
-        set_error("cudaMalloc failed");
-        batch_free(b);
-        return DGX_ERR_NOMEM;
+    put(oDt, dts.data(), sizeof(DtArgs) * n);
+    put(oCfl, cfl_items.data(), sizeof(int2) * cfl_items.size());
+    for (size_t c = 0; c < b->classes.size(); ++c) {
+        put(oArgs[c], args[c].data(), sizeof(StageArgs) * args[c].size());
+        put(oItems[c], items[c].data(), sizeof(int2) * items[c].size());
     }
-    if (cudaMemcpy(b->d_dt, dts.data(), sizeof(DtArgs) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(b->d_cfl_items, cfl_items.data(), sizeof(int2) * cfl_items.size(),
-                   cudaMemcpyHostToDevice) != cudaSuccess) {
+    b->d_scal = block_at<const double *>(b->block, oScal);
+    b->d_status = block_at<const unsigned int *>(b->block, oStat);
+    b->d_steps = block_at<const long long *>(b->block, oSteps);
+    b->d_dt = block_at<DtArgs>(b->block, oDt);
+    b->d_cfl_items = block_at<int2>(b->block, oCfl);
+    b->d_progress = block_at<double>(b->block, oProg);
+    b->h_progress.assign(4 * static_cast<size_t>(n), 0.0);
+    for (size_t c = 0; c < b->classes.size(); ++c) {
+        BatchClass &k = b->classes[c];
+        StageArgs *a0 = block_at<StageArgs>(b->block, oArgs[c]);
+        for (int st = 0; st < 4; ++st) k.d_args[st] = a0 + st * k.solves.size();
+        k.d_items = block_at<int2>(b->block, oItems[c]);
+    }
+    if (cudaMemcpy(b->block.base, stage.data(), upload, cudaMemcpyHostToDevice) != cudaSuccess) {
         set_error("batch upload failed");
         batch_free(b);
         return DGX_ERR_CUDA;
     }
     for (auto &k : b->classes) {
-        std::vector<int2> items;
-        for (size_t j = 0; j < k.solves.size(); ++j) {
-            const int ntiles = b->solvers[k.solves[j]]->mesh->d.num_tiles;
-            for (int t = 0; t < ntiles; ++t) items.push_back(make_int2(static_cast<int>(j), t));
-        }
-        k.n_items = static_cast<int>(items.size());
-        for (auto &p : k.d_args)
-            if (cudaMalloc(&p, sizeof(StageArgs) * k.solves.size()) != cudaSuccess) rc = DGX_ERR_NOMEM;
-        if (!rc && cudaMalloc(&k.d_items, sizeof(int2) * items.size()) != cudaSuccess) rc = DGX_ERR_NOMEM;
-        if (!rc && cudaMemcpy(k.d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice) !=
-                       cudaSuccess)
+        if (cudaStreamCreateWithFlags(&k.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&k.done, cudaEventDisableTiming) != cudaSuccess)
             rc = DGX_ERR_CUDA;
-        if (!rc && (cudaStreamCreateWithFlags(&k.stream, cudaStreamNonBlocking) != cudaSuccess ||
-                    cudaEventCreateWithFlags(&k.done, cudaEventDisableTiming) != cudaSuccess))
-            rc = DGX_ERR_CUDA;
-        if (!rc) rc = class_upload(b, k);
+        if (!rc) rc = class_configure(k);
         if (rc) break;
     }
     if (!rc && (cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess ||
@@ -388,7 +413,7 @@ int dgx_batch_progress(dgx_batch *b, double *t, double *dt, unsigned int *status
     const int n = static_cast<int>(b->solvers.size());
     progress_kernel<<<(n + 127) / 128, 128, 0, st>>>(b->d_scal, b->d_status, b->d_steps, n, b->d_progress);
     DGX_CHECK_LAUNCH();
-    DGX_TRY_CUDA(cudaMemcpyAsync(b->h_progress, b->d_progress, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st));
+    DGX_TRY_CUDA(cudaMemcpyAsync(b->h_progress.data(), b->d_progress, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st));
     DGX_TRY_CUDA(cudaStreamSynchronize(st));
     for (int i = 0; i < n; ++i) {
         if (t) t[i] = b->h_progress[4 * i];
