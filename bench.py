@@ -600,10 +600,19 @@ def main():
                          "contractions on the tensor cores (BF16x3)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and served sections")
+    ap.add_argument("--only", choices=["batched", "served"], default=None,
+                    help="run and print one section alone (for profiling it)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = dist_init()
+    if args.only:
+        import torch
+        torch.cuda.set_device(local)
+        from dgcuda_gb300 import build
+        build.build()
+        print(json.dumps(run_batched() if args.only == "batched" else run_served()), flush=True)
+        return
     if args.impl == "reference":
         out = run_reference(args, rank, world)
     else:
