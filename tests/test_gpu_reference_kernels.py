@@ -21,7 +21,7 @@ time is the same; the dissipation acts on small jumps).  Measured on GB300: FP64
 path 2e-13..7e-11, FP32 path 3e-7..2e-6.  Tolerances (relative L2 per conserved
 variable):
   FP64 path vs the reference          <= 1e-9
-  FP32 path vs the reference          <= 1e-5   (the benchmark spec's bound)
+  FP32 path vs the reference          <= 1e-5   (the FP32 path's accuracy bound)
 """
 import numpy as np
 import pytest
