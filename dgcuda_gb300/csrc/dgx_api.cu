@@ -226,7 +226,7 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
     a.nbr = m.nbr;
     a.halo_off = m.halo_off;
     a.halo_list = m.halo_list;
-    a.nslot = (3 * kTile + m.max_halo + 3) & ~3;   // keeps the prefetch area 16-byte aligned
+    a.nslot = 3 * kTile + m.max_halo;
     a.scal = s.scal;
     a.dt = dt;
     a.t = t;

@@ -293,13 +293,34 @@ __device__ __noinline__ void boundary_ghost(const StageArgs &a, int tag, int k, 
 }
 
 // Shared memory of one CTA: the side tables (for traces on a runtime side) and
-// the trace slots, slot-major with an odd stride: s_tr[slot * TSW + j*NV + n],
-// so a thread addresses a whole slot from one base register and threads
-// reading their own slots 3*tid + k (stride 3*TSW, odd) hit distinct banks.
+// the trace slots, slot-major: s_tr[slot_off(slot) + j*NV + n], so a thread
+// addresses a whole slot from one base register.  The 32 threads of a warp
+// write and read their own slots 3*tid + k together, so those slots must start
+// in 32 distinct banks.  An odd stride (NV*NQ1 | 1 words) does that.  For a
+// slot of 16 floats (Euler, p = 3) the slots are packed at stride 16 with one
+// word of padding per 6 slots instead: slot s starts at 16 s + s/6; the 16
+// threads whose slots have one parity start at s/6 = 16 w + u (u = 0..15, w
+// the warp) and the two parities 16 banks apart.  That takes nslot/6 words of
+// padding where the odd stride takes nslot: 1.7 KB less per CTA at 516 slots,
+// which keeps three CTAs of the order-3 Euler kernel on an SM with the widened
+// (132-value) prefetch planes of a mesh whose element count is not a multiple
+// of 4.
 template <int P, int NV>
 DGX_HD constexpr int side_table_words() { return (3 * ((num_modes(P) + 1) & ~1) * num_quad1(P) + 3) & ~3; }
 template <int P, int NV>
-DGX_HD constexpr int slot_words() { return (NV * num_quad1(P)) | 1; }
+DGX_HD constexpr bool slot_pad6() { return sizeof(R) == 4 && NV * num_quad1(P) == 16; }
+template <int P, int NV>
+DGX_HD constexpr int slot_words() { return slot_pad6<P, NV>() ? 16 : (NV * num_quad1(P)) | 1; }
+template <int P, int NV>
+DGX_HD __forceinline__ constexpr int slot_off(int slot) {
+    return slot * slot_words<P, NV>() + (slot_pad6<P, NV>() ? slot / 6 : 0);
+}
+// words of the slot area for nslot slots (a multiple of 4: what follows it is
+// 16-byte aligned)
+template <int P, int NV>
+DGX_HD constexpr size_t slot_area_words(int nslot) {
+    return (static_cast<size_t>(slot_off<P, NV>(nslot)) + 3) & ~static_cast<size_t>(3);
+}
 
 // Prefetched epilogue operands: per plane (variable x mode) of the base state
 // and of the accumulator, the tile's slice, widened to 16-byte boundaries (the
@@ -315,8 +336,7 @@ DGX_HD constexpr size_t prefetch_bytes(int plane) {
 
 template <int P, int NV>
 DGX_HD constexpr size_t stage_smem_bytes(int nslot, int prefetch) {
-    return 16 + sizeof(R) * (static_cast<size_t>(side_table_words<P, NV>()) +
-                             static_cast<size_t>(slot_words<P, NV>()) * nslot) +
+    return 16 + sizeof(R) * (static_cast<size_t>(side_table_words<P, NV>()) + slot_area_words<P, NV>(nslot)) +
            prefetch_bytes<P, NV>(prefetch);
 }
 
@@ -541,8 +561,7 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
     R *s_side = reinterpret_cast<R *>(smem_raw + 16);
     R *s_tr = s_side + side_table_words<P, NV>();
     const int nslot = a.nslot;
-    constexpr int TSW = slot_words<P, NV>();
-    R *s_pre = s_tr + static_cast<size_t>(TSW) * nslot;
+    R *s_pre = s_tr + slot_area_words<P, NV>(nslot);
 
     R dt;
     if (a.mode == 0) {
@@ -612,8 +631,8 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
                 R2 s2 = mk2(R(0), R(0));
 #pragma unroll
                 for (int i = 0; i < NP; ++i) s2 = fma2(c2[h][i], dup2(c_tab[L::SIDE + (k * NP + i) * NQ1 + j]), s2);
-                s_tr[(3 * tid + k) * TSW + j * NV + 2 * h] = s2.x;
-                s_tr[(3 * tid + k) * TSW + j * NV + 2 * h + 1] = s2.y;
+                s_tr[slot_off<P, NV>(3 * tid + k) + j * NV + 2 * h] = s2.x;
+                s_tr[slot_off<P, NV>(3 * tid + k) + j * NV + 2 * h + 1] = s2.y;
             }
     __syncthreads();   // s_side ready
 
@@ -646,8 +665,8 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
         for (int j = 0; j < NQ1; ++j)
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                s_tr[(3 * kTile + hh) * TSW + j * NV + 2 * h] = tr2[j][h].x;
-                s_tr[(3 * kTile + hh) * TSW + j * NV + 2 * h + 1] = tr2[j][h].y;
+                s_tr[slot_off<P, NV>(3 * kTile + hh) + j * NV + 2 * h] = tr2[j][h].x;
+                s_tr[slot_off<P, NV>(3 * kTile + hh) + j * NV + 2 * h + 1] = tr2[j][h].y;
             }
     }
 
@@ -753,8 +772,8 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
         const bool bnd = BND && word < 0;
         const int slot = bnd ? own : (word >> 1);
         const int il = bnd ? 1 : (word & 1);
-        const R *s_own = s_tr + own * TSW;
-        const R *s_nbr = s_tr + slot * TSW;
+        const R *s_own = s_tr + slot_off<P, NV>(own);
+        const R *s_nbr = s_tr + slot_off<P, NV>(slot);
         R2 Fh2[NQ1][2];
 #pragma unroll
         for (int j = 0; j < NQ1; ++j) {
@@ -817,8 +836,7 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
     float *s_side = reinterpret_cast<float *>(smem_raw + 16);   // [side][j][i], rows of NPP
     float *s_tr = s_side + side_table_words<P, NV>();
     const int nslot = a.nslot;
-    constexpr int TSW = slot_words<P, NV>();
-    float *s_pre = s_tr + static_cast<size_t>(TSW) * nslot;
+    float *s_pre = s_tr + slot_area_words<P, NV>(nslot);
 
     float dt;
     if (a.mode == 0) {
@@ -881,7 +899,7 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
             float2 acc = make_float2(0.0f, 0.0f);
 #pragma unroll
             for (int m = 0; m < NH; ++m) acc = fma2(c2[m], t2(T::SIDE + (k * NQ1 + j) * NPP + 2 * m), acc);
-            s_tr[(3 * tid + k) * TSW + j] = acc.x + acc.y;
+            s_tr[slot_off<P, NV>(3 * tid + k) + j] = acc.x + acc.y;
         }
     __syncthreads();   // s_side ready
 
@@ -897,7 +915,7 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
 #pragma unroll
             for (int m = 0; m < NH; ++m)
                 acc = fma2(cn2[m], *reinterpret_cast<const float2 *>(ts + j * NPP + 2 * m), acc);
-            s_tr[(3 * kTile + hh) * TSW + j] = acc.x + acc.y;
+            s_tr[slot_off<P, NV>(3 * kTile + hh) + j] = acc.x + acc.y;
         }
     }
 
@@ -943,8 +961,8 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
         const bool bnd = BND && word < 0;
         const int slot = bnd ? own : (word >> 1);
         const int il = bnd ? 1 : (word & 1);
-        const float *s_own = s_tr + own * TSW;
-        const float *s_nbr = s_tr + slot * TSW;
+        const float *s_own = s_tr + slot_off<P, NV>(own);
+        const float *s_nbr = s_tr + slot_off<P, NV>(slot);
         float2 Fh2[NQ1];
 #pragma unroll
         for (int j = 0; j < NQ1; ++j) {
@@ -996,10 +1014,9 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
     R *s_tr = s_side + side_table_words<P, NV>();
     const int nslot = a.nslot;
     // epilogue operands (base state, accumulator) of the tile, prefetched by the
-    // TMA engine while the element work runs; 16-byte aligned (side_table_words
-    // is a multiple of 4 and nslot of kTile-sized planes keeps alignment)
-    constexpr int TSW = slot_words<P, NV>();
-    R *s_pre = s_tr + static_cast<size_t>(TSW) * nslot;
+    // TMA engine while the element work runs; 16-byte aligned (the side tables
+    // and the slot area are multiples of 4 words)
+    R *s_pre = s_tr + slot_area_words<P, NV>(nslot);
 
     R dt;
     if (a.mode == 0) {
@@ -1075,7 +1092,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
                 R s = R(0);
 #pragma unroll
                 for (int i = 0; i < NP; ++i) s = fma(c[n][i], c_tab[L::SIDE + (k * NP + i) * NQ1 + j], s);
-                s_tr[(3 * tid + k) * TSW + j * NV + n] = s;
+                s_tr[slot_off<P, NV>(3 * tid + k) + j * NV + n] = s;
             }
     __syncthreads();   // s_side ready
 
@@ -1107,7 +1124,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
 #pragma unroll
         for (int j = 0; j < NQ1; ++j)
 #pragma unroll
-            for (int n = 0; n < NV; ++n) s_tr[(3 * kTile + h) * TSW + j * NV + n] = tr[j][n];
+            for (int n = 0; n < NV; ++n) s_tr[slot_off<P, NV>(3 * kTile + h) + j * NV + n] = tr[j][n];
     }
 
     R rhs[NV][NP];
@@ -1170,8 +1187,8 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
         const bool bnd = BND && word < 0;       // boundary side: this element is its left element
         const int slot = bnd ? own : (word >> 1);
         const int il = bnd ? 1 : (word & 1);
-        const R *s_own = s_tr + own * TSW;
-        const R *s_nbr = s_tr + slot * TSW;
+        const R *s_own = s_tr + slot_off<P, NV>(own);
+        const R *s_nbr = s_tr + slot_off<P, NV>(slot);
         R Fh[NQ1][NV];
 #pragma unroll
         for (int j = 0; j < NQ1; ++j) {

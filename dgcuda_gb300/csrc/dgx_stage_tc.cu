@@ -57,7 +57,7 @@ constexpr int kSmemHead = 128;   // barriers, tensor-memory address, flags
 template <int P, int NV>
 DGX_HD constexpr size_t tc_smem_bytes(int nslot, int prefetch) {
     return kSmemHead + tc_dims(P).bytes +
-           sizeof(R) * (static_cast<size_t>(side_table_words<P, NV>()) + static_cast<size_t>(slot_words<P, NV>()) * nslot) +
+           sizeof(R) * (static_cast<size_t>(side_table_words<P, NV>()) + slot_area_words<P, NV>(nslot)) +
            prefetch_bytes<P, NV>(prefetch);
 }
 
@@ -75,7 +75,6 @@ __global__ void __launch_bounds__(kTcThreads, 2) stage_kernel_tc(const StageArgs
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     using TC = TcCols<P, NV>;
     constexpr TcDims D = tc_dims(P);
-    constexpr int TSW = slot_words<P, NV>();
     // the two threads of a row split the variables (Euler: 0,1 | 2,3; advection:
     // the first thread), the volume points and the side points
     constexpr int VH = NV == 4 ? 2 : 1;
@@ -89,7 +88,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) stage_kernel_tc(const StageArgs
     unsigned char *s_img = smem_raw + kSmemHead;
     R *s_side = reinterpret_cast<R *>(s_img + D.bytes);
     R *s_tr = s_side + side_table_words<P, NV>();
-    R *s_pre = s_tr + static_cast<size_t>(TSW) * a.nslot;
+    R *s_pre = s_tr + slot_area_words<P, NV>(a.nslot);
     const int tile = blockIdx.x;
 
     R dt;
@@ -239,7 +238,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) stage_kernel_tc(const StageArgs
 #pragma unroll
             for (int j = 0; j < NQ1; ++j)
 #pragma unroll
-                for (int n = 0; n < NV; ++n) s_tr[(3 * kTile + hh) * TSW + j * NV + n] = tr[j][n];
+                for (int n = 0; n < NV; ++n) s_tr[slot_off<P, NV>(3 * kTile + hh) + j * NV + n] = tr[j][n];
         }
     }
 
@@ -266,7 +265,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) stage_kernel_tc(const StageArgs
             const int sp = s0 + ss;
             if (sp < SP) {
                 const int k = sp / NQ1, j = sp - k * NQ1;
-                s_tr[(3 * r + k) * TSW + j * NV + n] = (h == 0 ? d[NQ + ss] : d[NQ + SH + ss < D.nu ? NQ + SH + ss : 0]) + m0;
+                s_tr[slot_off<P, NV>(3 * r + k) + j * NV + n] = (h == 0 ? d[NQ + ss] : d[NQ + SH + ss < D.nu ? NQ + SH + ss : 0]) + m0;
             }
         }
     }
@@ -323,8 +322,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) stage_kernel_tc(const StageArgs
                 R UO[NV], UN[NV], UL[NV], UR[NV], Fh[NV];
 #pragma unroll
                 for (int n = 0; n < NV; ++n) {
-                    UO[n] = s_tr[own * TSW + j * NV + n];
-                    UN[n] = s_tr[slot * TSW + (NQ1 - 1 - j) * NV + n];
+                    UO[n] = s_tr[slot_off<P, NV>(own) + j * NV + n];
+                    UN[n] = s_tr[slot_off<P, NV>(slot) + (NQ1 - 1 - j) * NV + n];
                 }
                 if constexpr (BND) {
                     if (bnd) boundary_ghost<P, EQ>(a, word, k, j, e, UO, nx, ny, UN);
