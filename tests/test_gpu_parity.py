@@ -258,6 +258,31 @@ def test_config2_vortex_reduced(gpu, oracle_mod):
     assert rel_l2(sv.get_state(), ref).max() <= FP32_TOL
 
 
+@pytest.mark.parametrize("precision", [_ffi.FP32, _ffi.FP64], ids=["fp32", "fp64"])
+@pytest.mark.parametrize("kind,p,n", [("vortex", 3, 13), ("wave", 3, 12), ("vortex", 4, 11), ("advection", 3, 13)])
+def test_rk4_steps_parity_scrambled_tiles(kind, p, n, precision, gpu, oracle_mod):
+    """Several tiles of a scrambled mesh (E = 2 n^2 = 242..338: up to three
+    tiles whose halos hold most of their neighbours, so the trace slots past
+    the tile's own 3*128 are in use), E both a multiple of 4 and not: 10 RK4
+    steps against the oracle."""
+    orc = oracle_mod
+    m, eq, ic, params = make_case(kind, p, n=n, seed=7)
+    m = scramble(m, seed=11)
+    o = orc.Oracle(m, p, eq, _ffi.FLUX_LLF)
+    c0 = round_state(o.project(ic, params), precision)
+    dt = 0.3 * o.cfl_dt(c0) if eq == _ffi.EULER else 0.002
+    ref = c0.copy()
+    for s in range(10):
+        ref = o.step(ref, dt)
+    sv = Solver(m, p, eq, _ffi.FLUX_LLF, precision)
+    sv.set_state(c0)
+    sv.set_dt(dt)
+    k, _ = sv.run(max_steps=10)
+    assert k == 10
+    err = rel_l2(sv.get_state(), ref).max()
+    assert err <= (FP32_TOL if precision == _ffi.FP32 else 1e-11), err
+
+
 @pytest.mark.parametrize("precision", [_ffi.FP32, _ffi.FP64, _ffi.FP32_BF16X3], ids=["fp32", "fp64", "bf16x3"])
 @pytest.mark.parametrize("n", [8, 5, 9, 13])
 def test_prefetch_option_is_bitwise_neutral(n, precision, gpu):
