@@ -36,6 +36,9 @@ struct BatchClass {
     long long dofs = 0;
 };
 
+// elements per work item of the batched CFL kernel (8 per thread)
+constexpr int kCflItemElems = 2048;
+
 int num_sms() {
     static int sms = 0;
     if (!sms) {
@@ -271,6 +274,13 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
     std::vector<int2> cfl_items;
     for (int i = 0; i < n; ++i) {
         dts[i] = make_dt_args(solvers[i]->s, solvers[i]->mesh->d);
+        // one work item per kCflItemElems elements (the maximum is exact in any
+        // partition): the per-item reduction, atomics and argument loads then
+        // cost little beside the item's loads
+        if (dts[i].euler) {
+            const int want = (dts[i].E + kCflItemElems - 1) / kCflItemElems;
+            dts[i].nblocks = std::max(1, std::min(dts[i].nblocks, want));
+        }
         for (int blk = 0; blk < dts[i].nblocks; ++blk) cfl_items.push_back(make_int2(i, blk));
     }
     b->n_cfl_items = static_cast<int>(cfl_items.size());

@@ -214,6 +214,7 @@ __device__ void cfl_block(const DtArgs &a, int block, int nblocks) {
         // and FP64 division and square root run at a small fraction of the
         // FP32 rate on this GPU
         const T phi0 = static_cast<T>(a.phi0), gm = static_cast<T>(a.gamma);
+#pragma unroll 4
         for (int e = block * blockDim.x + threadIdx.x; e < a.E; e += nblocks * blockDim.x) {
             const T rho = c[e] * phi0;
             const T ru = c[NPE + e] * phi0;
