@@ -774,6 +774,15 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
         const int il = bnd ? 1 : (word & 1);
         const R *s_own = s_tr + slot_off<P, NV>(own);
         const R *s_nbr = s_tr + slot_off<P, NV>(slot);
+        // The flux from this element's side: (own, neighbour) states with the
+        // normal out of this element.  Swapping the states and negating the
+        // normal negates every operation of num_flux_euler_pair exactly
+        // (products and sums of negated operands, |un|, the max of the two
+        // wave speeds), so this is bitwise the side's flux (left, right, left
+        // normal) for the left element and its negation for the right one, and
+        // -len/2 times its lift is bitwise the left/right form's contribution.
+        const R sgn = il ? R(1) : R(-1);
+        const R nxo = sgn * nx, nyo = sgn * ny;
         R2 Fh2[NQ1][2];
 #pragma unroll
         for (int j = 0; j < NQ1; ++j) {
@@ -788,12 +797,12 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
                 if (bnd) boundary_ghost<P, EQ>(a, word, k, j, e, UO, nx, ny, UN);
             }
 #pragma unroll
-            for (int n = 0; n < NV; ++n) Ulr[n] = il ? mk2(UO[n], UN[n]) : mk2(UN[n], UO[n]);
-            num_flux_euler_pair(Ulr, nx, ny, llf, g, Fh);
+            for (int n = 0; n < NV; ++n) Ulr[n] = mk2(UO[n], UN[n]);
+            num_flux_euler_pair(Ulr, nxo, nyo, llf, g, Fh);
             Fh2[j][0] = mk2(Fh[0], Fh[1]);
             Fh2[j][1] = mk2(Fh[2], Fh[3]);
         }
-        const R2 sg2 = dup2(il ? -hl : hl);
+        const R2 sg2 = dup2(-hl);
 #pragma unroll
         for (int h = 0; h < 2; ++h)
 #pragma unroll
@@ -963,6 +972,11 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
         const int il = bnd ? 1 : (word & 1);
         const float *s_own = s_tr + slot_off<P, NV>(own);
         const float *s_nbr = s_tr + slot_off<P, NV>(slot);
+        // the flux from this element's side, (own, neighbour) with the normal
+        // out of this element: bitwise the left/right form for the left
+        // element and its negation for the right one (as in stage_tile_pair)
+        const float sgn = il ? 1.0f : -1.0f;
+        const float nxo = sgn * nx, nyo = sgn * ny;
         float2 Fh2[NQ1];
 #pragma unroll
         for (int j = 0; j < NQ1; ++j) {
@@ -970,12 +984,11 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
             if constexpr (BND) {
                 if (bnd) boundary_ghost<P, EQ>(a, word, k, j, e, UO, nx, ny, UN);
             }
-            const float UL[1] = {il ? UO[0] : UN[0]}, UR[1] = {il ? UN[0] : UO[0]};
             float Fh[1];
-            num_flux<EQ>(UL, UR, nx, ny, llf, a.gammaf, ax, ay, Fh);
+            num_flux<EQ>(UO, UN, nxo, nyo, llf, a.gammaf, ax, ay, Fh);
             Fh2[j] = dup2(Fh[0]);
         }
-        const float2 sg2 = dup2(il ? -hl : hl);
+        const float2 sg2 = dup2(-hl);
 #pragma unroll
         for (int m = 0; m < NH; ++m) {
             float2 acc = make_float2(0.0f, 0.0f);
