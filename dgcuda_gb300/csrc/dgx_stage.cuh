@@ -549,8 +549,10 @@ __device__ __forceinline__ void num_flux_euler_pair(const R2 (&Ulr)[4], R nx, R 
 // (rho, rho u) and (rho v, E), so that every basis contraction (traces, point
 // values, volume projection, lift) issues one paired FMA per two variables.
 // Each lane performs the scalar kernel's fused multiply-adds with the same
-// operands in the same order, so the results are bitwise stage_tile's; the
-// fluxes and the epilogue stay scalar.
+// operands in the same order, and the side flux's own-side form is the
+// scalar kernel's left/right form negated exactly where the element is the
+// right one, so the results are bitwise stage_tile's; the fluxes and the
+// epilogue stay scalar.
 template <int P, bool BND>
 __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int tile, unsigned char *smem_raw,
                                                 const unsigned parity) {
