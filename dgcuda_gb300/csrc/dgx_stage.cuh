@@ -389,6 +389,11 @@ __device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, uns
     return pre;
 }
 
+template <int K>
+struct IntC {
+    static constexpr int value = K;
+};
+
 // Mass inverse and the RK combination of the stage (time_integrator.cu:194-218,
 // 445-464, 622-700): k = dt/J rhs, then per mode of the kernel
 //   0 k;  1 u2 = c + k/2, acc = c + k/6;  2/3 u = c + alpha k, acc += k/3;
@@ -406,9 +411,6 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     const R sc = dt * invJ;
     R *__restrict__ out = static_cast<R *>(a.out);
-    const R *pc = nullptr, *pacc = nullptr;   // base state / accumulator of this element
-    size_t pstride = SE;
-    int sm = 0;   // prefetched: plane p's slice starts (p * sm) mod kPreAlign values into its copy
     if (pre) {
         if (!mbar_wait_bounded(bar, parity, 1ll << 26)) {
             // the copies did not land in time: report, wait once more for the
@@ -417,14 +419,51 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
             mbar_wait_bounded(bar, parity, 1ll << 28);
             return pre;
         }
-        pc = s_pre + row;
-        pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * a.prefetch) + row;
-        pstride = a.prefetch;
-        sm = static_cast<int>(SE & (kPreAlign - 1));
-    } else {
-        pc = static_cast<const R *>(a.c) + e;
-        pacc = static_cast<const R *>(a.acc) + e;
     }
+    // Modes 2..4 read this element's base state and accumulator, value pi =
+    // (variable, mode) of each: kind 0 from global memory; kind 1 from the
+    // prefetched planes (a.prefetch values each; plane pi's slice starts
+    // (pi * (E mod kPreAlign)) mod kPreAlign values into its copy); kind 2 from
+    // kTile-value planes (E a multiple of kPreAlign), at compile-time offsets.
+    auto rk_tail = [&](auto kind) {
+        constexpr int K = decltype(kind)::value;
+        const R *pc, *pacc;
+        if constexpr (K == 0) {
+            pc = static_cast<const R *>(a.c) + e;
+            pacc = static_cast<const R *>(a.acc) + e;
+        } else {
+            pc = s_pre + row;
+            pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * a.prefetch) + row;
+        }
+        const int pstride = a.prefetch, sm = static_cast<int>(SE & (kPreAlign - 1));
+        auto at = [&](const R *p, int pi) -> R {
+            if constexpr (K == 2) return p[pi * kTile];
+            else if constexpr (K == 1) return p[pi * pstride + ((pi * sm) & (kPreAlign - 1))];
+            else return p[pi * SE];
+        };
+        if (a.mode == 4) {   // c = acc + k4/6
+#pragma unroll
+            for (int n = 0; n < VC; ++n)
+#pragma unroll
+                for (int i = 0; i < NP; ++i) {
+                    const size_t o = ((V0 + n) * NP + i) * SE + e;
+                    out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], at(pacc, (V0 + n) * NP + i));
+                }
+        } else {             // 2: u3 = c + k2/2, acc += k2/3;  3: u4 = c + k3, acc += k3/3
+            R *__restrict__ acc = static_cast<R *>(a.acc);
+            const R alpha = a.mode == 2 ? R(0.5) : R(1);
+#pragma unroll
+            for (int n = 0; n < VC; ++n)
+#pragma unroll
+                for (int i = 0; i < NP; ++i) {
+                    const R kk = sc * rhs[n][i];
+                    const size_t o = ((V0 + n) * NP + i) * SE + e;
+                    const int pi = (V0 + n) * NP + i;
+                    out[o] = fma(alpha, kk, at(pc, pi));
+                    acc[o] = fma(R(1.0 / 3.0), kk, at(pacc, pi));
+                }
+        }
+    };
     switch (a.mode) {
     case 0:
 #pragma unroll
@@ -445,34 +484,13 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
             }
         break;
     }
-    case 2:     // u3 = c + k2/2, acc += k2/3
-    case 3: {   // u4 = c + k3,   acc += k3/3
-        R *__restrict__ acc = static_cast<R *>(a.acc);
-        const R alpha = a.mode == 2 ? R(0.5) : R(1);
-#pragma unroll
-        for (int n = 0; n < VC; ++n)
-#pragma unroll
-            for (int i = 0; i < NP; ++i) {
-                const R kk = sc * rhs[n][i];
-                const size_t o = ((V0 + n) * NP + i) * SE + e;
-                const int pi = (V0 + n) * NP + i;
-                const size_t po = pi * pstride + ((pi * sm) & (kPreAlign - 1));
-                out[o] = fma(alpha, kk, pc[po]);
-                acc[o] = fma(R(1.0 / 3.0), kk, pacc[po]);
-            }
+    case 2:
+    case 3:
+    case 4:
+        if (!pre) rk_tail(IntC<0>{});
+        else if (a.prefetch == kTile) rk_tail(IntC<2>{});
+        else rk_tail(IntC<1>{});
         break;
-    }
-    case 4: {   // c = acc + k4/6
-#pragma unroll
-        for (int n = 0; n < VC; ++n)
-#pragma unroll
-            for (int i = 0; i < NP; ++i) {
-                const size_t o = ((V0 + n) * NP + i) * SE + e;
-                const int pi = (V0 + n) * NP + i;
-                out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], pacc[pi * pstride + ((pi * sm) & (kPreAlign - 1))]);
-            }
-        break;
-    }
     case 5: {   // out = u + alpha k (RK2 first stage, forward Euler)
         const R alpha = R(a.alpha);
 #pragma unroll
