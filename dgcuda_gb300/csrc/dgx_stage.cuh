@@ -352,7 +352,7 @@ __device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, uns
                                                int tid) {
     constexpr int NP = num_modes(P);
     const int E = a.E;
-    const size_t SE = static_cast<size_t>(E);
+    const size_t SE = static_cast<unsigned>(E);   // zero-extended: plane offsets k*SE are 32x32-bit products
     const bool pre = a.prefetch && a.mode >= 2 && a.mode <= 4;
     if (pre && tid < 32) {
         // order this CTA's earlier generic-proxy accesses of the shared memory
@@ -594,7 +594,7 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
     const int tid = threadIdx.x;
     const int e = tile * kTile + tid;
     const bool live = e < E;
-    const size_t SE = static_cast<size_t>(E);
+    const size_t SE = static_cast<unsigned>(E);   // zero-extended: plane offsets k*SE are 32x32-bit products
     const R g = a.gammaf, ax = a.axf, ay = a.ayf;
     const int llf = a.flux == DGX_FLUX_LLF;
     const R *__restrict__ u = static_cast<const R *>(a.u);
@@ -878,7 +878,7 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
     const int tid = threadIdx.x;
     const int e = tile * kTile + tid;
     const bool live = e < E;
-    const size_t SE = static_cast<size_t>(E);
+    const size_t SE = static_cast<unsigned>(E);   // zero-extended: plane offsets k*SE are 32x32-bit products
     const float ax = a.axf, ay = a.ayf;
     const int llf = a.flux == DGX_FLUX_LLF;
     const float *__restrict__ u = static_cast<const float *>(a.u);
@@ -1062,7 +1062,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
     const int tid = threadIdx.x;
     const int e = tile * kTile + tid;
     const bool live = e < E;
-    const size_t SE = static_cast<size_t>(E);
+    const size_t SE = static_cast<unsigned>(E);   // zero-extended: plane offsets k*SE are 32x32-bit products
     // physics constants in the kernel's precision (FP32 copies avoid FP64 conversions)
     const R g = sizeof(R) == 4 ? R(a.gammaf) : R(a.gamma);
     const R ax = sizeof(R) == 4 ? R(a.axf) : R(a.ax);
