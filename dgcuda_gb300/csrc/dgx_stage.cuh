@@ -411,6 +411,7 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
     constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
     const R sc = dt * invJ;
     R *__restrict__ out = static_cast<R *>(a.out);
+    R *__restrict__ oe = out + e;   // (array + element) + plane * E: one wide multiply-add per access
     if (pre) {
         if (!mbar_wait_bounded(bar, parity, 1ll << 26)) {
             // the copies did not land in time: report, wait once more for the
@@ -446,21 +447,20 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
             for (int n = 0; n < VC; ++n)
 #pragma unroll
                 for (int i = 0; i < NP; ++i) {
-                    const size_t o = ((V0 + n) * NP + i) * SE + e;
-                    out[o] = fma(R(1.0 / 6.0), sc * rhs[n][i], at(pacc, (V0 + n) * NP + i));
+                    const int pi = (V0 + n) * NP + i;
+                    oe[pi * SE] = fma(R(1.0 / 6.0), sc * rhs[n][i], at(pacc, pi));
                 }
         } else {             // 2: u3 = c + k2/2, acc += k2/3;  3: u4 = c + k3, acc += k3/3
-            R *__restrict__ acc = static_cast<R *>(a.acc);
+            R *__restrict__ ae = static_cast<R *>(a.acc) + e;
             const R alpha = a.mode == 2 ? R(0.5) : R(1);
 #pragma unroll
             for (int n = 0; n < VC; ++n)
 #pragma unroll
                 for (int i = 0; i < NP; ++i) {
                     const R kk = sc * rhs[n][i];
-                    const size_t o = ((V0 + n) * NP + i) * SE + e;
                     const int pi = (V0 + n) * NP + i;
-                    out[o] = fma(alpha, kk, at(pc, pi));
-                    acc[o] = fma(R(1.0 / 3.0), kk, at(pacc, pi));
+                    oe[pi * SE] = fma(alpha, kk, at(pc, pi));
+                    ae[pi * SE] = fma(R(1.0 / 3.0), kk, at(pacc, pi));
                 }
         }
     };
@@ -472,15 +472,15 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
             for (int i = 0; i < NP; ++i) out[((V0 + n) * NP + i) * SE + e] = sc * rhs[n][i];
         break;
     case 1: {   // u2 = c + k1/2, acc = c + k1/6
-        R *__restrict__ acc = static_cast<R *>(a.acc);
+        R *__restrict__ ae = static_cast<R *>(a.acc) + e;
 #pragma unroll
         for (int n = 0; n < VC; ++n)
 #pragma unroll
             for (int i = 0; i < NP; ++i) {
                 const R kk = sc * rhs[n][i];
-                const size_t o = ((V0 + n) * NP + i) * SE + e;
-                out[o] = fma(R(0.5), kk, c[n][i]);
-                acc[o] = fma(R(1.0 / 6.0), kk, c[n][i]);
+                const size_t o = ((V0 + n) * NP + i) * SE;
+                oe[o] = fma(R(0.5), kk, c[n][i]);
+                ae[o] = fma(R(1.0 / 6.0), kk, c[n][i]);
             }
         break;
     }
@@ -602,12 +602,15 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
     for (int t = tid; t < 3 * NP * NQ1; t += kTile) s_side[t] = c_tab[L::SIDE + t];
     const bool pre = issue_prefetch<P, NV>(a, tile, bar, s_pre, tid);
 
+    // plane-major arrays are addressed as (array + element) + plane * E: one
+    // wide multiply-add per access
+    const R *__restrict__ ue = u + (live ? e : 0);
     R2 c2[2][NP];
 #pragma unroll
     for (int h = 0; h < 2; ++h)
 #pragma unroll
         for (int i = 0; i < NP; ++i)
-            c2[h][i] = live ? mk2(__ldg(u + ((2 * h) * NP + i) * SE + e), __ldg(u + ((2 * h + 1) * NP + i) * SE + e))
+            c2[h][i] = live ? mk2(__ldg(ue + ((2 * h) * NP + i) * SE), __ldg(ue + ((2 * h + 1) * NP + i) * SE))
                             : mk2(R(0), R(0));
 
     int sw[3];
@@ -616,12 +619,14 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
         const int *__restrict__ nbr = a.nbr;
         const R *__restrict__ fn = static_cast<const R *>(a.fn);
         const int ee = live ? e : 0;
+        const int *__restrict__ nbe = nbr + ee;
+        const R *__restrict__ fne = fn + ee;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            sw[k] = __ldg(nbr + k * SE + ee);
-            snx[k] = __ldg(fn + (3 * k + 0) * SE + ee);
-            sny[k] = __ldg(fn + (3 * k + 1) * SE + ee);
-            shl[k] = __ldg(fn + (3 * k + 2) * SE + ee);
+            sw[k] = __ldg(nbe + k * SE);
+            snx[k] = __ldg(fne + (3 * k + 0) * SE);
+            sny[k] = __ldg(fne + (3 * k + 1) * SE);
+            shl[k] = __ldg(fne + (3 * k + 2) * SE);
         }
     }
 
@@ -634,7 +639,7 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
         for (int h = 0; h < 2; ++h)
 #pragma unroll
             for (int i = 0; i < NP; ++i)
-                cn2[h][i] = mk2(__ldg(u + ((2 * h) * NP + i) * SE + ne), __ldg(u + ((2 * h + 1) * NP + i) * SE + ne));
+                cn2[h][i] = mk2(__ldg(u + ne + ((2 * h) * NP + i) * SE), __ldg(u + ne + ((2 * h + 1) * NP + i) * SE));
     }
 
     // own traces on the three sides (constant-bank side tables)
@@ -664,8 +669,8 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
             for (int h = 0; h < 2; ++h)
 #pragma unroll
                 for (int i = 0; i < NP; ++i)
-                    cn2[h][i] = mk2(__ldg(u + ((2 * h) * NP + i) * SE + ne),
-                                            __ldg(u + ((2 * h + 1) * NP + i) * SE + ne));
+                    cn2[h][i] = mk2(__ldg(u + ne + ((2 * h) * NP + i) * SE),
+                                    __ldg(u + ne + ((2 * h + 1) * NP + i) * SE));
         }
         const R *ts = s_side + (hw & 3) * NP * NQ1;
         R2 tr2[NQ1][2];
@@ -699,11 +704,12 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
     R invJ = R(0), xr = R(0), yr = R(0), xs = R(0), ys = R(0);
     if (live) {
         const R *__restrict__ geo = static_cast<const R *>(a.geo);
-        invJ = __ldg(geo + e);
-        xr = __ldg(geo + SE + e);
-        yr = __ldg(geo + 2 * SE + e);
-        xs = __ldg(geo + 3 * SE + e);
-        ys = __ldg(geo + 4 * SE + e);
+        const R *__restrict__ ge = geo + e;
+        invJ = __ldg(ge);
+        xr = __ldg(ge + SE);
+        yr = __ldg(ge + 2 * SE);
+        xs = __ldg(ge + 3 * SE);
+        ys = __ldg(ge + 4 * SE);
         const R2 ys2 = dup2(ys), xr2 = dup2(xr), nxs2 = dup2(-xs), nyr2 = dup2(-yr);
         // point values of the pair h at the point whose table values t(i) gives
         // metric terms (fx ys - fy xs, fy xr - fx yr) per variable pair
