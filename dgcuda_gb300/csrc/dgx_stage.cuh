@@ -893,11 +893,12 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
     for (int t = tid; t < 3 * NQ1 * NPP; t += kTile) s_side[t] = c_tabT[T::SIDE + t];
     const bool pre = issue_prefetch<P, NV>(a, tile, bar, s_pre, tid);
 
+    const float *__restrict__ ue = u + (live ? e : 0);   // (array + element) + plane * E
     float2 c2[NH];
 #pragma unroll
     for (int m = 0; m < NH; ++m) {
-        const float lo = live ? __ldg(u + (2 * m) * SE + e) : 0.0f;
-        const float hi = (live && 2 * m + 1 < NP) ? __ldg(u + (2 * m + 1) * SE + e) : 0.0f;
+        const float lo = live ? __ldg(ue + (2 * m) * SE) : 0.0f;
+        const float hi = (live && 2 * m + 1 < NP) ? __ldg(ue + (2 * m + 1) * SE) : 0.0f;
         c2[m] = make_float2(lo, hi);
     }
 
@@ -907,12 +908,14 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
         const int *__restrict__ nbr = a.nbr;
         const float *__restrict__ fn = static_cast<const float *>(a.fn);
         const int ee = live ? e : 0;
+        const int *__restrict__ nbe = nbr + ee;
+        const float *__restrict__ fne = fn + ee;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            sw[k] = __ldg(nbr + k * SE + ee);
-            snx[k] = __ldg(fn + (3 * k + 0) * SE + ee);
-            sny[k] = __ldg(fn + (3 * k + 1) * SE + ee);
-            shl[k] = __ldg(fn + (3 * k + 2) * SE + ee);
+            sw[k] = __ldg(nbe + k * SE);
+            snx[k] = __ldg(fne + (3 * k + 0) * SE);
+            sny[k] = __ldg(fne + (3 * k + 1) * SE);
+            shl[k] = __ldg(fne + (3 * k + 2) * SE);
         }
     }
 
@@ -922,7 +925,7 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
     auto gather = [&](int ne) {
 #pragma unroll
         for (int m = 0; m < NH; ++m)
-            cn2[m] = make_float2(__ldg(u + (2 * m) * SE + ne), 2 * m + 1 < NP ? __ldg(u + (2 * m + 1) * SE + ne) : 0.0f);
+            cn2[m] = make_float2(__ldg(u + ne + (2 * m) * SE), 2 * m + 1 < NP ? __ldg(u + ne + (2 * m + 1) * SE) : 0.0f);
     };
     if (hw >= 0) gather(hw >> 2);
 
@@ -962,8 +965,9 @@ __device__ __forceinline__ bool stage_tile_adv_pair(const StageArgs &a, const in
     if (live) {
         const float *__restrict__ geo = static_cast<const float *>(a.geo);
         invJ = __ldg(geo + e);
-        const float xr = __ldg(geo + SE + e), yr = __ldg(geo + 2 * SE + e);
-        const float xs = __ldg(geo + 3 * SE + e), ys = __ldg(geo + 4 * SE + e);
+        const float *__restrict__ ge = geo + e;
+        const float xr = __ldg(ge + SE), yr = __ldg(ge + 2 * SE);
+        const float xs = __ldg(ge + 3 * SE), ys = __ldg(ge + 4 * SE);
         // p = 4 unrolled (measured 8 % faster), the lower orders rolled (p = 3
         // unrolled was 10 % slower)
 #pragma unroll(P == 4 ? NQ : 1)
