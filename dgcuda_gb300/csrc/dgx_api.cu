@@ -553,6 +553,7 @@ int dgx_solver_destroy(dgx_solver *sv) {
     if (!sv) return DGX_ERR_INVALID;
     block_free(sv->block);
     if (sv->s.prev) cudaFree(sv->s.prev);
+    if (sv->s.tot_scratch) cudaFree(sv->s.tot_scratch);
     if (sv->mesh) mesh_release(sv->mesh);
     delete sv;
     return DGX_OK;

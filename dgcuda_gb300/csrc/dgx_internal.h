@@ -177,6 +177,7 @@ struct SolverDev {
     int limiter = 0;                   // DGX_OPT_LIMITER: limit every stage's output (p = 1)
     unsigned long long *chg_bits = nullptr;   // largest coefficient change (double bits)
     void *prev = nullptr;              // dgx_run_steady: the state before the step (on demand)
+    double *tot_scratch = nullptr;     // dgx_conserved_totals: E terms + kReduceLen + 1 (on demand)
     int bc_kind = 0, bc_ic = 0;        // boundary ghost states (StageArgs)
     double bc_state[4] = {0, 0, 0, 0};
     double bc_params[8] = {0, 0, 0, 0, 0, 0, 0, 0};

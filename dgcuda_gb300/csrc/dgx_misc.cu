@@ -386,15 +386,21 @@ int launch_batch_dt(const DtArgs *args, const int2 *items, int n_items, cudaStre
 
 int conserved_totals(SolverDev &s, const MeshDev &m, double *out, cudaStream_t st) {
     const int E = m.num_elem;
-    double *terms = nullptr;
     const int len = kReduceLen;
-    double *scratch = nullptr;
-    DGX_TRY_CUDA(cudaMalloc(&terms, sizeof(double) * E));
-    if (cudaMalloc(&scratch, sizeof(double) * (len + 1)) != cudaSuccess) {
-        cudaFree(terms);
-        set_error("cudaMalloc failed");
-        return DGX_ERR_NOMEM;
+    // per-element terms and the reduction's partials: allocated on the first
+    // call and kept with the solver, so a loop that checks conservation every
+    // step neither allocates nor waits for the device in cudaFree
+    if (!s.tot_scratch) {
+        void *p = nullptr;
+        if (cudaMalloc(&p, sizeof(double) * (static_cast<size_t>(E) + len + 1)) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("cudaMalloc of %zu bytes for the totals failed", sizeof(double) * (static_cast<size_t>(E) + len + 1));
+            return DGX_ERR_NOMEM;
+        }
+        s.tot_scratch = static_cast<double *>(p);
     }
+    double *terms = s.tot_scratch;
+    double *scratch = s.tot_scratch + E;
     const double phi0 = tables(s.order).phi[0];
     int rc = DGX_OK;
     for (int n = 0; n < s.nv && rc == DGX_OK; ++n) {
@@ -409,8 +415,6 @@ int conserved_totals(SolverDev &s, const MeshDev &m, double *out, cudaStream_t s
         rc = reduce_host(terms, E, 0, scratch, len, &sum, st);
         out[n] = sum * phi0 * 0.5;
     }
-    cudaFree(terms);
-    cudaFree(scratch);
     return rc;
 }
 

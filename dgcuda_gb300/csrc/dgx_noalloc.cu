@@ -7,8 +7,6 @@
 // device memory, or a latency-critical loop that cannot afford the implicit
 // device synchronisation of cudaFree.  dgx_conserved_totals_static() computes
 // the same totals with its scratch in a file-scope static device array instead.
-#include <mutex>
-
 #include "dgx_internal.h"
 
 namespace dgx {
@@ -23,22 +21,15 @@ constexpr int kNoAllocMaxBlocks = 8192;    // partial sums per variable
 // on every device that loads the library, until the process exits.
 __device__ __align__(256) double g_totals_scratch[4 * kNoAllocMaxBlocks];
 
-std::mutex g_sym_mu;
-double *g_sym_ptr[64] = {nullptr};
-
 // Host code cannot use g_totals_scratch as an address: look up its device
-// address once per device, with that device current.
+// address with the calling thread's current device.  The lookup is repeated on
+// every call rather than cached, so a host that resets the device
+// (cudaDeviceReset, which discards the module and its static arrays) and keeps
+// calling gets the array of the new context, not a dangling address.
 int scratch_address(double **out) {
-    int dev = 0;
-    DGX_TRY_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) { set_error("device index %d out of range", dev); return DGX_ERR_UNSUPPORTED; }
-    std::lock_guard<std::mutex> lk(g_sym_mu);
-    if (!g_sym_ptr[dev]) {
-        void *p = nullptr;
-        DGX_TRY_CUDA(cudaGetSymbolAddress(&p, g_totals_scratch));
-        g_sym_ptr[dev] = static_cast<double *>(p);
-    }
-    *out = g_sym_ptr[dev];
+    void *p = nullptr;
+    DGX_TRY_CUDA(cudaGetSymbolAddress(&p, g_totals_scratch));
+    *out = static_cast<double *>(p);
     return DGX_OK;
 }
 
@@ -90,6 +81,8 @@ using namespace dgx;
 
 extern "C" int dgx_conserved_totals_static(const dgx_solver *sv, const void *state, double *out,
                                            void *stream) {
+    // the handle is const for the caller; its launch counter is bookkeeping
+    dgx_solver *counted = const_cast<dgx_solver *>(sv);
     if (!sv || !state || !out) { set_error("NULL argument"); return DGX_ERR_INVALID; }
     const MeshDev &m = sv->mesh->d;
     const SolverDev &s = sv->s;
@@ -115,5 +108,6 @@ extern "C" int dgx_conserved_totals_static(const dgx_solver *sv, const void *sta
     DGX_CHECK_LAUNCH();
     totals_final_kernel<<<1, kNoAllocThreads, 0, st>>>(partial, nblocks, s.nv, tables(s.order).phi[0] * 0.5, out);
     DGX_CHECK_LAUNCH();
+    counted->launches += 2;
     return DGX_OK;
 }

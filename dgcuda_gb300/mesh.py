@@ -23,7 +23,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 __all__ = ["Mesh", "periodic_square", "scramble", "dirichlet_square", "unit_draws", "write_pmsh",
-           "read_pmsh", "read_gmsh", "tag_boundary", "from_triangles", "annulus"]
+           "read_pmsh", "read_gmsh", "gmsh_to_pmsh", "tag_boundary", "from_triangles", "annulus"]
 
 
 def _splitmix64(x: np.ndarray) -> np.ndarray:
@@ -268,24 +268,35 @@ def scramble(m: Mesh, seed: int = 0, rotate: bool = True, swap: bool = True,
 # File formats
 # ---------------------------------------------------------------------------
 
-def write_pmsh(mesh: Mesh, path: str) -> None:
-    """Write the reference's .pmsh text format (src/2d/genmesh.py:290-308), with
-    full-precision coordinates; side end points are the left element's."""
+def _pmsh_text(E, S, V, es, side_xy, le, re, ls, rs, fixed6: bool) -> str:
+    """The .pmsh text (src/2d/genmesh.py:290-308): E, then per element its six
+    vertex coordinates and three side indices; S, then per side its two end
+    points, left and right element and side numbers.  fixed6 writes the
+    coordinates as the reference's converter does ("%lf": six decimals,
+    correctly rounded), else full precision (shortest round-trip form)."""
+    num = (lambda x: "%f" % x) if fixed6 else (lambda x: repr(float(x)))
+    out = [f"{E}"]
+    for e in range(E):
+        out.append(" ".join(num(x) for x in V[:, e]) + f" {es[0, e]} {es[1, e]} {es[2, e]}")
+    out.append(f"{S}")
+    for s in range(S):
+        out.append(" ".join(num(x) for x in side_xy[:, s]) + f" {le[s]} {re[s]} {ls[s]} {rs[s]}")
+    return "\n".join(out) + "\n"
+
+
+def write_pmsh(mesh: Mesh, path: str, fixed6: bool = False) -> None:
+    """Write the reference's .pmsh text format (src/2d/genmesh.py:290-308); side
+    end points are the left element's.  Coordinates at full precision, or with
+    fixed6 at the reference converter's six decimals ("%lf")."""
     E, S = mesh.num_elem, mesh.num_sides
     V = np.stack(mesh.vertices())
     es = np.stack(mesh.elem_sides())
     P = V.reshape(3, 2, E)
+    le, ls = mesh.left_elem.astype(np.int64), mesh.left_side.astype(np.int64)
+    side_xy = np.concatenate([P[ls, :, le].T, P[(ls + 1) % 3, :, le].T]) if S else np.zeros((4, 0))
     with open(path, "w") as f:
-        f.write(f"{E}\n")
-        for e in range(E):
-            f.write(" ".join(repr(float(x)) for x in V[:, e]) + f" {es[0, e]} {es[1, e]} {es[2, e]}\n")
-        f.write(f"{S}\n")
-        for s in range(S):
-            L, ls = int(mesh.left_elem[s]), int(mesh.left_side[s])
-            a = [float(x) for x in P[ls, :, L]]
-            b = [float(x) for x in P[(ls + 1) % 3, :, L]]
-            f.write(f"{a[0]!r} {a[1]!r} {b[0]!r} {b[1]!r} {L} {int(mesh.right_elem[s])} {ls} "
-                    f"{int(mesh.right_side[s])}\n")
+        f.write(_pmsh_text(E, S, V, es, side_xy, mesh.left_elem, mesh.right_elem, mesh.left_side,
+                           mesh.right_side, fixed6))
 
 
 def read_pmsh(path: str) -> Mesh:
@@ -303,20 +314,19 @@ def read_pmsh(path: str) -> Mesh:
 BOUNDARY_TAGS = {10000: -1, 20000: -2, 30000: -3}   # physical tags of genmesh.py:170-180
 
 
-def read_gmsh(path_or_text: str, boundary_tags=None) -> Mesh:
-    """Gmsh v2.2 ASCII .msh -> Mesh, the job of the reference's Python-2
-    converter (src/2d/genmesh.py:11-310) restated for Python 3.  Triangles
-    become elements (clockwise ones are reordered to counter-clockwise);
-    sides are matched by their vertex pair, the first element to meet a side
-    is its left element; line elements tag boundary sides by their physical
-    group (10000 reflecting -> -1, 20000 outflow -> -2, 30000 inflow -> -3);
-    boundary sides are sorted first, in the order -1, -2, -3."""
-    tags = dict(BOUNDARY_TAGS if boundary_tags is None else boundary_tags)
+def _parse_gmsh(path_or_text: str):
+    """Gmsh v2.2 ASCII: node coordinates (n, 2), triangles as node-index triples
+    and lines as (node pair, physical tag), both in file order.  Nodes are
+    addressed by their file order; element lines are read by type and tag
+    count (the reference's converter reads lines of 7 and 8 fields, the same
+    elements for the two-tag files Gmsh writes, src/2d/genmesh.py:36-58)."""
     text = path_or_text
     if "\n" not in path_or_text:
         with open(path_or_text) as f:
             text = f.read()
-    lines = text.splitlines()
+    lines = [ln.strip() for ln in text.splitlines()]
+    if "$Nodes" not in lines:
+        raise ValueError("not a Gmsh v2 file (no $Nodes section)")
     i = lines.index("$Nodes")
     n_nodes = int(lines[i + 1])
     node_id, xy = {}, []
@@ -324,22 +334,149 @@ def read_gmsh(path_or_text: str, boundary_tags=None) -> Mesh:
         parts = lines[i + 2 + k].split()
         node_id[int(parts[0])] = k
         xy.append((float(parts[1]), float(parts[2])))
-    xy = np.array(xy)
     i = lines.index("$Elements")
     n_el = int(lines[i + 1])
-    tris, bnd = [], {}
+    tris, segs = [], []
     for k in range(n_el):
         parts = [int(x) for x in lines[i + 2 + k].split()]
         etype, ntags = parts[1], parts[2]
         phys = parts[3] if ntags > 0 else 0
         nodes = [node_id[x] for x in parts[3 + ntags:]]
         if etype == 2:
-            a, b, c = nodes[:3]
-            J = (xy[b, 0] - xy[a, 0]) * (xy[c, 1] - xy[a, 1]) - (xy[c, 0] - xy[a, 0]) * (xy[b, 1] - xy[a, 1])
-            tris.append((a, c, b) if J < 0 else (a, b, c))
+            tris.append(tuple(nodes[:3]))
         elif etype == 1:
-            bnd[frozenset(nodes[:2])] = tags.get(phys, -1)
-    return from_triangles(xy, tris, lambda a, b: bnd.get(frozenset((a, b)), -1), kind="gmsh")
+            segs.append(((nodes[0], nodes[1]), phys))
+    return np.array(xy, dtype=np.float64).reshape(-1, 2), tris, segs
+
+
+def _number_sides(tris, tag_of, unmatched):
+    """Sides of a triangulation in the reference converter's numbering
+    (src/2d/genmesh.py:84-241).  Elements are visited in order; a side of
+    element i that an earlier element created (its vertex pair in either
+    direction) gets i as its right element and k as its right side number;
+    then each of the element's new sides k = 0, 1, 2 (V1V2, V2V3, V3V1) is
+    appended with i as its left element.  tag_of(a, b) is the boundary tag of a
+    new side (or None); a side that no second element meets and that has no
+    tag gets `unmatched` as its right element.  Returns es[E][3], le, re, ls,
+    rs (lists)."""
+    E = len(tris)
+    es = [[0, 0, 0] for _ in range(E)]
+    le, re, ls, rs = [], [], [], []
+    created = {}
+    for i, t in enumerate(tris):
+        edges = ((t[0], t[1]), (t[1], t[2]), (t[2], t[0]))
+        new = [True, True, True]
+        for k, (a, b) in enumerate(edges):
+            for key in ((a, b), (b, a)):
+                q = created.get(key)
+                if q is not None:
+                    new[k] = False
+                    re[q], rs[q], es[i][k] = i, k, q
+        for k, (a, b) in enumerate(edges):
+            if new[k]:
+                q = len(le)
+                created[(a, b)] = q
+                tag = tag_of(a, b)
+                le.append(i); ls.append(k); re.append(unmatched if tag is None else tag); rs.append(0)
+                es[i][k] = q
+    return es, le, re, ls, rs
+
+
+def _boundary_first(es, le, re, ls, rs, order=(-1, -2, -3)):
+    """Move the boundary sides to the front, all of tag -1, then -2, then -3,
+    by the reference converter's exchanges (src/2d/genmesh.py:244-284): a
+    running slot j starts at 0; for each side i with the tag (in index order)
+    the sides at i and j trade places -- the elements of the side at j are
+    pointed at i, the left element of the side at i at j -- and j advances.
+    The reference also points "the right element" of the side at j at i when
+    that side is a boundary side, which Python's negative indexing turns into
+    a write into the side lists of the mesh's last elements; that write is
+    left out here (on every .msh/.pmsh pair the reference ships, later
+    exchanges overwrite those entries and the files agree byte for byte).
+    Modifies the lists in place."""
+    j = 0
+    for tag in order:
+        for i in range(len(le)):
+            if re[i] != tag:
+                continue
+            es[le[j]][ls[j]] = i
+            if re[j] >= 0:
+                es[re[j]][rs[j]] = i
+            es[le[i]][ls[i]] = j
+            for arr in (le, re, ls, rs):
+                arr[i], arr[j] = arr[j], arr[i]
+            j += 1
+
+
+def _tagger(segs, tags):
+    """tag_of(a, b) for the sides of a triangulation: the tag of the physical
+    group of a line element on the side (either direction), the last such
+    line with a known group winning (genmesh.py:170-180); None without one."""
+    on_side = {}
+    for (a, b), phys in segs:
+        if phys in tags:
+            on_side[(a, b)] = on_side[(b, a)] = tags[phys]
+    return lambda a, b: on_side.get((a, b))
+
+
+def read_gmsh(path_or_text: str, boundary_tags=None) -> Mesh:
+    """Gmsh v2.2 ASCII .msh -> Mesh, the job of the reference's Python-2
+    converter (src/2d/genmesh.py:11-310) restated for Python 3, for solving.
+    Triangles become elements in file order; sides are numbered as the
+    reference numbers them (``_number_sides``) and its boundary sides sorted
+    first, -1, -2, -3, by its exchanges (``_boundary_first``); line elements
+    tag boundary sides by their physical group (10000 reflecting -> -1, 20000
+    outflow -> -2, 30000 inflow -> -3).  For counter-clockwise triangles and
+    tagged boundaries the arrays equal those of the reference's .pmsh (see
+    ``gmsh_to_pmsh``) at full precision.  Two cases differ, where the
+    reference's file would not be a valid mesh: a clockwise triangle has its
+    first two vertices exchanged in that element only (the reference exchanges
+    the two vertices' coordinates for the whole mesh), and a boundary side
+    without a known tag becomes reflecting (-1) (the reference leaves element 0
+    as its right element)."""
+    tags = dict(BOUNDARY_TAGS if boundary_tags is None else boundary_tags)
+    xy, tris, segs = _parse_gmsh(path_or_text)
+    ccw = []
+    for a, b, c in tris:
+        J = (xy[b, 0] - xy[a, 0]) * (xy[c, 1] - xy[a, 1]) - (xy[c, 0] - xy[a, 0]) * (xy[b, 1] - xy[a, 1])
+        ccw.append((b, a, c) if J < 0 else (a, b, c))
+    tag_of = _tagger(segs, tags)
+    return from_triangles(xy, ccw, lambda a, b: tag_of(a, b) or -1, kind="gmsh")
+
+
+def gmsh_to_pmsh(msh_path_or_text: str, pmsh_path: str | None = None, boundary_tags=None) -> str:
+    """The reference's mesh converter (src/2d/genmesh.py:11-310, Python 2) as a
+    Python 3 function: Gmsh v2.2 .msh -> the .pmsh text its solvers read,
+    byte for byte what the reference's converter writes, written to pmsh_path
+    when given and returned.  Kept alike on purpose, for files that must
+    match the reference's: the six-decimal coordinates ("%lf"); a triangle
+    with a negative Jacobian (computed from the coordinates as they stand when
+    it is visited) exchanges the coordinates of its first two vertices in the
+    shared vertex list, which moves them for every element that uses them
+    (genmesh.py:95-100); a side that no second element meets and no tagged line
+    lies on keeps element 0 and side 0 as its right neighbour (genmesh.py:
+    69-75).  ``read_gmsh`` gives the solvable mesh instead."""
+    tags = dict(BOUNDARY_TAGS if boundary_tags is None else boundary_tags)
+    xy, tris, segs = _parse_gmsh(msh_path_or_text)
+    xy = xy.copy()
+    for a, b, c in tris:
+        J = (xy[b, 0] - xy[a, 0]) * (xy[c, 1] - xy[a, 1]) - (xy[c, 0] - xy[a, 0]) * (xy[b, 1] - xy[a, 1])
+        if J < 0:
+            xy[[a, b]] = xy[[b, a]]
+    es, le, re, ls, rs = _number_sides(tris, _tagger(segs, tags), unmatched=0)
+    _boundary_first(es, le, re, ls, rs)
+    T = np.array(tris, dtype=np.int64).reshape(-1, 3)
+    E, S = T.shape[0], len(le)
+    V = np.stack([xy[T[:, 0], 0], xy[T[:, 0], 1], xy[T[:, 1], 0], xy[T[:, 1], 1],
+                  xy[T[:, 2], 0], xy[T[:, 2], 1]]) if E else np.zeros((6, 0))
+    ends = [(T[le[s], ls[s]], T[le[s], (ls[s] + 1) % 3]) for s in range(S)]
+    side_xy = np.array([[xy[a, 0], xy[a, 1], xy[b, 0], xy[b, 1]] for a, b in ends]).T.reshape(4, S)
+    text = _pmsh_text(E, S, V, np.array(es, dtype=np.int64).reshape(-1, 3).T, side_xy, le, re, ls, rs,
+                      fixed6=True)
+    if pmsh_path:
+        with open(pmsh_path, "w") as f:
+            f.write(text)
+    return text
 
 
 def tag_boundary(mesh: Mesh, fn) -> Mesh:
@@ -357,42 +494,27 @@ def tag_boundary(mesh: Mesh, fn) -> Mesh:
 
 def from_triangles(xy, tris, boundary_tag, kind: str = "triangles") -> Mesh:
     """Vertices ``xy[n, 2]`` and counter-clockwise triangles ``tris[E, 3]`` (vertex
-    indices) -> Mesh.  Sides are matched by their vertex pair, the first
-    element to meet a side is its left element; an unmatched side is a
-    boundary side tagged ``boundary_tag(a, b)`` (its vertex indices, in the left
-    element's order).  Boundary sides come first, in the order -1, -2, -3, as
-    the reference's converter sorts them (genmesh.py:244-284)."""
+    indices) -> Mesh, with the sides numbered as the reference's converter
+    numbers them (``_number_sides``: matched by their vertex pair, the first
+    element to meet a side is its left element).  A side that no second
+    element meets is a boundary side tagged ``boundary_tag(a, b)`` (its vertex
+    indices, in the left element's order), with right side number 0 as in the
+    reference's files.  Boundary sides come first, -1, -2, -3, moved there by
+    the reference's exchanges (``_boundary_first``, genmesh.py:244-284)."""
     xy = np.asarray(xy, dtype=np.float64)
-    T = np.asarray(tris, dtype=np.int64)
-    E = T.shape[0]
-    es = np.zeros((E, 3), dtype=np.int64)
-    le, re, ls, rs, ends = [], [], [], [], []
-    side_of = {}
-    for e in range(E):
-        t = T[e]
-        for k in range(3):
-            a, b = int(t[k]), int(t[(k + 1) % 3])
-            key = (a, b) if a < b else (b, a)
-            if key in side_of:
-                q = side_of.pop(key)
-                re[q], rs[q] = e, k
-            else:
-                q = len(le)
-                side_of[key] = q
-                le.append(e); ls.append(k); re.append(-1); rs.append(-1); ends.append((a, b))
-            es[e, k] = q
-    for q in side_of.values():   # sides met once: boundary sides
-        re[q] = int(boundary_tag(*ends[q]))
-    le, re, ls, rs = (np.array(x, dtype=np.int64) for x in (le, re, ls, rs))
-    order = np.concatenate([np.nonzero(re == t)[0] for t in (-1, -2, -3)] + [np.nonzero(re >= 0)[0]])
-    if order.size != le.size:
-        raise ValueError("boundary tags must be -1, -2 or -3")
-    inv = np.empty_like(order)
-    inv[order] = np.arange(order.size)
-    es = inv[es]
+    T = np.asarray(tris, dtype=np.int64).reshape(-1, 3)
+    open_side = -(1 << 30)
+    es, le, re, ls, rs = _number_sides([tuple(int(v) for v in t) for t in T], lambda a, b: None, open_side)
+    for q in range(len(le)):
+        if re[q] == open_side:   # sides met once: boundary sides
+            tag = int(boundary_tag(int(T[le[q], ls[q]]), int(T[le[q], (ls[q] + 1) % 3])))
+            if tag not in (-1, -2, -3):
+                raise ValueError("boundary tags must be -1, -2 or -3")
+            re[q] = tag
+    _boundary_first(es, le, re, ls, rs)
+    es = np.array(es, dtype=np.int64).reshape(-1, 3)
     V = [xy[T[:, 0], 0], xy[T[:, 0], 1], xy[T[:, 1], 0], xy[T[:, 1], 1], xy[T[:, 2], 0], xy[T[:, 2], 1]]
-    m = Mesh(*V, es[:, 0], es[:, 1], es[:, 2], le[order], re[order], ls[order], rs[order],
-             meta=dict(kind=kind))
+    m = Mesh(*V, es[:, 0], es[:, 1], es[:, 2], le, re, ls, rs, meta=dict(kind=kind))
     m.check()
     return m
 

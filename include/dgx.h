@@ -195,25 +195,30 @@ int dgx_run(dgx_solver *solver, double t_end, int max_steps, int *steps, double 
 /* Current simulation time and last dt (synchronises the stream). */
 int dgx_time(dgx_solver *solver, double *t, double *dt, void *stream);
 int dgx_reset_time(dgx_solver *solver, double t);
-/* Conserved totals  int u_n dx  in FP64 (deterministic device reduction). */
+/* Conserved totals  int u_n dx  in FP64 (deterministic device reduction).
+ * The first call on a solver allocates its scratch (8 bytes per element plus
+ * 32 KiB), kept until the solver is destroyed; later calls allocate nothing.
+ * Synchronous (the totals are host doubles). */
 int dgx_conserved_totals(dgx_solver *solver, double *out, void *stream);
 /* Conserved totals without allocating.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc: a serving loop held to a fixed
  * device-memory budget, an application whose own allocator owns the device
  * memory, or a latency-critical loop that cannot take the device-wide
  * synchronisation of cudaFree.  dgx_conserved_totals allocates scratch on
- * every call; this variant keeps its scratch in one static device array of
+ * its first call on a solver; this variant keeps its scratch in one static device array of
  * 256 KiB (4 variables x 8192 partial sums), held on every device that loads
  * the library until the process exits.  It allocates nothing and frees nothing.
  *   state  the solver's state layout and precision, device memory
  *          (e.g. dgx_state_device_ptr)
  *   out    num_vars doubles, device-accessible, written by the GPU
  * Meshes above DGX_TOTALS_STATIC_MAX_ELEMS elements are refused with
- * DGX_ERR_INVALID.  Asynchronous on `stream`.  The first call on a device
- * looks up the array's device address, so make that first call before any
- * stream capture.  All calls share the one array: calls that overlap on the
- * GPU (different streams, no ordering between them) race and give wrong
- * totals. */
+ * DGX_ERR_INVALID.  Asynchronous on `stream`.  Every call looks up the
+ * array's device address on the current device (so a cudaDeviceReset between
+ * calls is harmless); the first lookup on a device may load the library's
+ * device code, so make the first call before any stream capture.  Its two
+ * kernel launches count in dgx_launch_count.  All calls share the one array:
+ * calls that overlap on the GPU (different streams, no ordering between them)
+ * race and give wrong totals. */
 #define DGX_TOTALS_STATIC_MAX_ELEMS 16777216
 int dgx_conserved_totals_static(const dgx_solver *solver, const void *state, double *out,
                                 void *stream);

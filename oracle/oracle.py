@@ -35,20 +35,31 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def install_ref(reference_root: str = "/root/reference") -> bool:
+def env_reference_root() -> str | None:
+    """The reference tree named by the environment variable DGX_REFERENCE_ROOT
+    (the directory holding src/2d), or None when it is unset or absent."""
+    root = os.environ.get("DGX_REFERENCE_ROOT", "")
+    return root if root and os.path.isdir(root) else None
+
+
+def install_ref(reference_root: str | None = None) -> bool:
     """Copy the reference's Euler sources the harnesses compile (unmodified) to
-    baseline/_ref/src/2d, for machines without the reference tree."""
-    if not os.path.isdir(reference_root):
+    baseline/_ref/src/2d, for machines without the reference tree.
+    reference_root defaults to DGX_REFERENCE_ROOT; False without a tree."""
+    reference_root = reference_root or env_reference_root()
+    if not reference_root or not os.path.isdir(reference_root):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref-src", f"REF={reference_root}"], check=True)
     return True
 
 
-def build_ref(reference_root: str = "/root/reference") -> str | None:
-    """Compile the reference's own CPU Euler loops, from the reference tree or
-    the installed copy; the binary path or None."""
-    r = subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={reference_root}"],
-                       capture_output=True, text=True)
+def build_ref(reference_root: str | None = None) -> str | None:
+    """Compile the reference's own CPU Euler loops, from the reference tree
+    (reference_root, else DGX_REFERENCE_ROOT) or the installed copy under
+    baseline/_ref; the binary path or None."""
+    reference_root = reference_root or env_reference_root()
+    cmd = ["make", "-s", "-C", HERE, "ref"] + ([f"REF={reference_root}"] if reference_root else [])
+    r = subprocess.run(cmd, capture_output=True, text=True)
     return REF_BIN if r.returncode == 0 and os.path.exists(REF_BIN) else None
 
 

@@ -109,7 +109,9 @@ def run_case(ref_bin, name, build, p, ic, params, dt, nsteps):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else orc.env_reference_root()
+    if not ref_root:
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT (or set DGX_REFERENCE_ROOT)")
     ref_bin = orc.build_ref(ref_root)
     if ref_bin is None:
         raise SystemExit(f"reference tree not found at {ref_root}")
