@@ -37,13 +37,14 @@ sys.path.insert(0, ROOT)
 
 METRIC = "DOF-updates/s on 1 GB300, served/batched vs plain at L2≤1e-5; p50/p99 latency"
 UNIT = "DOF-updates/s"
-def workload(n: int) -> dict:
-    """Labels of the density-wave workload on the 2 x n^2 mesh."""
+def workload(n: int, precision: str = "fp32") -> dict:
+    """Labels of the density-wave workload on the 2 x n^2 mesh, computed in
+    `precision` (the arithmetic of the arm that reports it)."""
     mb = 2 * n * n * 40 * 4 / 1e6
     return dict(workload=f"euler_density_wave_2x{n}^2_p3", equation="euler", order=3,
                 num_elem=2 * n * n, mesh=f"periodic 2x{n}^2, jitter 0.15h, seed 12347",
                 ic="rho=1+0.2 sin(2pi(x+y)), u=v=1, p=1, gamma=1.4", flux="LLF",
-                integrator="RK4, CFL 0.7 on device", precision="fp32",
+                integrator="RK4, CFL 0.7 on device", precision=precision,
                 l2_flush=f"inputs larger than L2 (4 state vectors x {mb:.1f} MB)" if 4 * mb > 129
                 else f"inputs of 4 x {mb:.1f} MB (not larger than L2)")
 
@@ -153,7 +154,7 @@ def run_reference(args, rank, world):
     wave = (0.2, 1.0, 1.0, 1.0, 1.0)
     out = {"metric": METRIC, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64", "data": "synthetic", "config": workload(args.mesh_n), "impl": "reference"}
+           "dtype": "f64", "data": "synthetic", "config": workload(args.mesh_n, "fp64"), "impl": "reference"}
     if orc.build_ref() is not None:
         cores = os.cpu_count() or 1
         # size each process's sub-problem so that the timed steps take about a minute
@@ -370,6 +371,7 @@ def run_batched(steps: int = 20):
         info = bt.info()
         opts = bt.class_options()
     bt.close()
+    accuracy = _sample_accuracy(specs, solvers, 2 * (3 + steps))
     for sv in solvers:
         sv.close()
     return {"workload": "256 solves: equation 50/50, N log-uniform [16,512] (2N^2 triangles), "
@@ -379,7 +381,36 @@ def run_batched(steps: int = 20):
             "plain_value": dofs / (plain_ms * 1e-3), "plain_ms_per_step": plain_ms,
             "speedup_vs_plain": plain_ms / batch_ms, "classes": info["classes"],
             "work_items": info["items"], "launches_per_step": launches / steps,
-            "tuned_options": opts, "unit": UNIT}
+            "tuned_options": opts, "accuracy": accuracy, "unit": UNIT}
+
+
+def _sample_accuracy(specs, solvers, nsteps, every: int = 16):
+    """Relative L2 per conserved variable of a sample of the FP32 solves
+    (every `every`-th) against the same solve in FP64 (the FP64 path, held to
+    1e-11 of the CPU oracle by the parity tests), both `nsteps` CFL steps from
+    the same initial state; the FP32 run's dt comes from its FP32 state, so the
+    two runs' times differ by FP32 rounding."""
+    from dgcuda_gb300 import _ffi
+    from dgcuda_gb300.solver import DeviceMesh, Solver
+    worst, rows = [0.0] * 4, []
+    for k in range(0, len(specs), every):
+        sp, sv = specs[k], solvers[k]
+        dm = DeviceMesh.periodic_square(sp["n"], sp["lx"], sp["ly"], sp["jitter"], sp["seed"])
+        ref = Solver(dm, sp["order"], sp["equation"], _ffi.FLUX_LLF, _ffi.FP64, 1.4)
+        ref.project(sp["ic"], sp["params"])
+        ref.set_dt(None, cfl=0.7)
+        ref.run(max_steps=nsteps)
+        a, b = sv.get_state(), ref.get_state()
+        ref.close()
+        nv = a.shape[0]
+        err = [float(np.linalg.norm(a[n] - b[n]) / np.linalg.norm(b[n])) for n in range(nv)]
+        for n in range(nv):
+            worst[n] = max(worst[n], err[n])
+        rows.append({"solve": k, "n": sp["n"], "order": sp["order"],
+                     "equation": "euler" if sp["equation"] == _ffi.EULER else "advection", "rel_l2": err})
+    return {"reference": f"the same solve in FP64 on the GPU, {nsteps} CFL steps from the same initial state",
+            "max_rel_l2_per_variable": worst, "max_rel_l2": max(worst), "meets_1e-5": max(worst) <= 1e-5,
+            "sample": rows}
 
 
 def run_served(rates=(50, 200, 1000, 2000, 0), count: int = 400):
@@ -501,6 +532,22 @@ def run_bf16x3(mesh, args, stage_bytes, peak, dofs, fp32_ms):
             "accuracy": acc}
 
 
+def run_fp64(mesh, args, dofs, steps: int = 10):
+    """The same workload in FP64 (DGX_FP64, the reference's precision): step
+    time, for a same-precision comparison with the reference's own CUDA solver
+    rebuilt for sm_103a (the reference arm's `reference_gpu`, FP64)."""
+    import torch
+    from dgcuda_gb300 import _ffi
+    sv = density_wave_solver(mesh, _ffi.FP64)
+    stream = torch.cuda.Stream()
+    ms, stage_ms, launches, _, _ = time_steps(sv, steps, 3, stream, 1)
+    sv.close()
+    return {"value": dofs / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": steps, "dtype": "f64",
+            "gpu_launches": launches,
+            "what": "the FP64 path (scalar FP64 stage kernel, FP64 state) on the same workload; compare with "
+                    "the reference arm's reference_gpu (the reference's CUDA solver, FP64)"}
+
+
 def run_ours(args, rank, world, local):
     import torch
     torch.cuda.set_device(local)
@@ -582,6 +629,7 @@ def run_ours(args, rank, world, local):
         out["cpu_baseline"] = cpu_baseline_sample()
     if not args.no_extra and prec == _ffi.FP32:
         out["bf16x3"] = run_bf16x3(mesh, args, stage_bytes, peak, dofs, ms_step)
+        out["fp64"] = run_fp64(mesh, args, dofs)
         out["accuracy"] = run_accuracy(args.mesh_n)
         out["batched"] = run_batched()
         out["served"] = run_served()

@@ -21,7 +21,8 @@ FLUX_CENTRAL, FLUX_LLF = 0, 1
 FP32, FP32_BF16X3, FP64 = 0, 1, 2
 RK4, RK2, FE = 0, 1, 2
 DT_FIXED, DT_CFL = 0, 1
-OPT_PREFETCH, OPT_STAGE_TIME, OPT_LIMITER = 1, 2, 3
+OPT_PREFETCH, OPT_STAGE_TIME, OPT_LIMITER, OPT_HOOK_MATH = 1, 2, 3, 4
+HOOK_MATH_DOUBLE, HOOK_MATH_REFERENCE = 0, 1
 STAGE_TIME_EXACT, STAGE_TIME_REFERENCE = 0, 1
 BC_NONE, BC_FREESTREAM, BC_EXACT, BC_PROBLEM = 0, 1, 2, 3
 IC_GAUSSIAN, IC_POLY, IC_DENSITY_WAVE, IC_VORTEX, IC_CONSTANT = 0, 1, 2, 3, 4

@@ -240,6 +240,7 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
     a.alpha = (mode == 5 && s.integrator == DGX_RK2) ? 0.5 : 1.0;
     a.bc_kind = s.bc_kind;
     a.bc_ic = s.bc_ic;
+    a.hook_float = s.hook_math == DGX_HOOK_MATH_REFERENCE ? 1 : 0;
     for (int i = 0; i < 4; ++i) a.bc_state[i] = s.bc_state[i];
     for (int i = 0; i < 8; ++i) a.bc_params[i] = s.bc_params[i];
     a.V = m.V;
@@ -810,6 +811,13 @@ int dgx_solver_set_option(dgx_solver *sv, int option, int value) {
             return DGX_ERR_INVALID;
         }
         sv->s.stage_time = value;
+        return DGX_OK;
+    case DGX_OPT_HOOK_MATH:
+        if (value != DGX_HOOK_MATH_DOUBLE && value != DGX_HOOK_MATH_REFERENCE) {
+            set_error("unknown hook arithmetic %d", value);
+            return DGX_ERR_INVALID;
+        }
+        sv->s.hook_math = value;
         return DGX_OK;
     default: set_error("unknown option %d", option); return DGX_ERR_INVALID;
     }

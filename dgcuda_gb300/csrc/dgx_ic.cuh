@@ -28,7 +28,10 @@ __device__ inline void threepoint_shock(const double *P, double g, double *U) {
     U[3] = 0.5 * U[0] * P[0] * P[0] + 1.0 / (g - 1.0);
 }
 
-__device__ inline void ic_eval(int ic, const double *P, double g, double x, double y, double *U) {
+// ref_float: the FP32 powers of the reference's problem file where it calls
+// powf (the supersonic vortex, supersonic.cu:30,35); FP64 pow otherwise
+__device__ inline void ic_eval(int ic, const double *P, double g, double x, double y, double *U,
+                               bool ref_float = false) {
     const double pi = 3.14159265358979323846;
     switch (ic) {
     case DGX_IC_GAUSSIAN: {
@@ -59,13 +62,16 @@ __device__ inline void ic_eval(int ic, const double *P, double g, double x, doub
         U[0] = g; U[1] = U[0] * P[0]; U[2] = 0.0;
         U[3] = 0.5 * U[0] * P[0] * P[0] + 1.0 / (g - 1.0);
         break;
-    case DGX_IC_SUPERSONIC_VORTEX: {   // supersonic.cu:28-38 (pow for its powf)
+    case DGX_IC_SUPERSONIC_VORTEX: {   // supersonic.cu:28-38 (pow, or with ref_float its powf)
         const double r = sqrt(x * x + y * y), th = atan(y / x);
         const double A = P[1] != 0.0 ? P[1] : 0.5 * (g - 1.0) * P[0] * P[0];
-        U[0] = pow(1.0 + A * (1.0 - 1.0 / (r * r)), 2.5);
+        const double base = 1.0 + A * (1.0 - 1.0 / (r * r));
+        U[0] = ref_float ? static_cast<double>(powf(static_cast<float>(base), 2.5f)) : pow(base, 2.5);
         U[1] = U[0] * sin(th) * P[0] / r;
         U[2] = U[0] * -cos(th) * P[0] / r;
-        const double p = (1.0 / g) * pow(U[0], g);
+        const double p = (1.0 / g) * (ref_float ? static_cast<double>(powf(static_cast<float>(U[0]),
+                                                                           static_cast<float>(g)))
+                                                : pow(U[0], g));
         U[3] = 0.5 * U[0] * (P[0] * P[0] / (r * r)) + p * (1.0 / (g - 1.0));
         break;
     }

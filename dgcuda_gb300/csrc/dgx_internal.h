@@ -175,6 +175,7 @@ struct SolverDev {
     int stage_time = DGX_STAGE_TIME_EXACT;   // DGX_OPT_STAGE_TIME
     int prefetch = 1;                  // DGX_OPT_PREFETCH
     int limiter = 0;                   // DGX_OPT_LIMITER: limit every stage's output (p = 1)
+    int hook_math = DGX_HOOK_MATH_DOUBLE;   // DGX_OPT_HOOK_MATH
     unsigned long long *chg_bits = nullptr;   // largest coefficient change (double bits)
     void *prev = nullptr;              // dgx_run_steady: the state before the step (on demand)
     double *tot_scratch = nullptr;     // dgx_conserved_totals: E terms + kReduceLen + 1 (on demand)
@@ -230,6 +231,7 @@ struct StageArgs {
     // state bc_state (Euler), 2 exact initial condition bc_ic / bc_params
     // translated by a*t (advection)
     int bc_kind, bc_ic;
+    int hook_float;            // DGX_BC_PROBLEM ghost states with the reference's FP32 sqrtf/powf
     double bc_state[4];
     double bc_params[8];
     const double *V;           // element vertices V1x, V1y, V2x, V2y, V3x, V3y [6][E] (FP64)

@@ -247,7 +247,10 @@ __device__ __noinline__ void boundary_ghost(const StageArgs &a, int tag, int k, 
                 const double c0 = a.bc_ic == DGX_IC_CYLINDER ? 0.5 : 0.0;
                 x -= c0;
                 y -= c0;
-                const double d = sqrt(x * x + y * y);
+                // the radius in FP64, or as the reference's hooks take it, sqrtf
+                // of the FP64 sum (cylinder.cu:100, supersonic.cu:100)
+                const double d = a.hook_float ? static_cast<double>(sqrtf(static_cast<float>(x * x + y * y)))
+                                              : sqrt(x * x + y * y);
                 const R Nx = static_cast<R>(x / d), Ny = static_cast<R>(y / d);
                 const R tm = UO[1] * Ny - UO[2] * Nx;
                 UN[0] = UO[0];
@@ -262,7 +265,7 @@ __device__ __noinline__ void boundary_ghost(const StageArgs &a, int tag, int k, 
                 if (tag == -2 || x < prm[0] * t * cos(ang) + tan(ang)) threepoint_shock(prm, g, U);
                 else ic_eval(DGX_IC_THREEPOINT, prm, g, x, y, U);
             } else {
-                ic_eval(a.bc_ic, prm, g, x, y, U);
+                ic_eval(a.bc_ic, prm, g, x, y, U, a.hook_float != 0);
             }
             for (int n = 0; n < 4; ++n) UN[n] = static_cast<R>(U[n]);
             return;

@@ -295,8 +295,18 @@ int dgx_solver_set_boundary(dgx_solver *solver, int kind, int ic, const double *
  *                     reference's limiter hook after each stage,
  *                     time_integrator.cu:302,332,363); p = 1 only, single
  *                     solves (batches refuse such solvers); 0 (default): off. */
-enum dgx_option { DGX_OPT_PREFETCH = 1, DGX_OPT_STAGE_TIME = 2, DGX_OPT_LIMITER = 3 };
+/*   DGX_OPT_HOOK_MATH the arithmetic of the DGX_BC_PROBLEM ghost states:
+ *                     DGX_HOOK_MATH_DOUBLE (default) FP64 throughout;
+ *                     DGX_HOOK_MATH_REFERENCE the FP32 square roots and powers
+ *                       of the reference's problem files (sqrtf of the radius in
+ *                       the radial reflections, cylinder.cu:100 and
+ *                       supersonic.cu:100; powf in the supersonic vortex's
+ *                       state, supersonic.cu:30,35), for callers that need the
+ *                       reference's numbers near those boundaries.  The two
+ *                       differ by FP32 rounding in the ghost states. */
+enum dgx_option { DGX_OPT_PREFETCH = 1, DGX_OPT_STAGE_TIME = 2, DGX_OPT_LIMITER = 3, DGX_OPT_HOOK_MATH = 4 };
 enum dgx_stage_time { DGX_STAGE_TIME_EXACT = 0, DGX_STAGE_TIME_REFERENCE = 1 };
+enum dgx_hook_math { DGX_HOOK_MATH_DOUBLE = 0, DGX_HOOK_MATH_REFERENCE = 1 };
 int dgx_solver_set_option(dgx_solver *solver, int option, int value);
 /* Number of CUDA kernels this solver has launched so far. */
 int dgx_launch_count(const dgx_solver *solver, long long *count);

@@ -6,9 +6,13 @@ ref-gpu` from the reference's unmodified sources (src/2d/conservation,
 src/2d/2dadvec and src/2d/{time_integrator,quadrature,basis}.cu, from the
 reference tree or the copy `make -C oracle ref-src` installs under
 baseline/_ref) with `ref_gpu_harness.cu` as their problem file and driver.
-`run` hands the Euler solver a periodic mesh and an initial state and lets the
-reference's time_integrate_rk4 (src/2d/conservation/time_integrator.cu:221-434)
-advance to t_end with its CFL rule; `run_advection` lets the advection solver's
+`run` hands the Euler solver a mesh and an initial state and lets the
+reference's time_integrate_rk4 (src/2d/conservation/time_integrator.cu:221-434),
+or time_integrate_rk2 (:466-614), advance to t_end with its CFL rule: on
+periodic meshes with the harness's own hooks, or with the boundary hooks of the
+reference's cylinder (src/2d/conservation/euler/cylinder/cylinder.cu) or
+supersonic-vortex (euler/supersonic/supersonic.cu) problem file, compiled in
+(`problem`); `run_advection` lets the advection solver's
 time_integrate_rk4 (src/2d/time_integrator.cu:89-315) take a number of steps of
 a fixed dt (a = (1,1), central flux).  Both return the state, the steps taken
 and the time.
@@ -25,31 +29,38 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BIN = os.path.join(HERE, "_ref", "ref_gpu_euler")
 BIN_ADVEC = os.path.join(HERE, "_ref", "ref_gpu_advec")
+BIN_PROBLEM = {"cylinder": os.path.join(HERE, "_ref", "ref_gpu_cylinder"),
+               "supersonic": os.path.join(HERE, "_ref", "ref_gpu_supersonic")}
 
 
 def build() -> str | None:
     """Build the harnesses if their sources are at hand; the Euler binary's path
     or None."""
-    if not (os.path.exists(BIN) and os.path.exists(BIN_ADVEC)):
-        r = subprocess.run(["make", "-s", "-C", HERE, "ref-gpu"], capture_output=True, text=True)
+    bins = [BIN, BIN_ADVEC] + list(BIN_PROBLEM.values())
+    if not all(os.path.exists(b) for b in bins):
+        r = subprocess.run(["make", "-s", "-j4", "-C", HERE, "ref-gpu"], capture_output=True, text=True)
         if r.returncode != 0:
             return None
-    return BIN if os.path.exists(BIN) and os.path.exists(BIN_ADVEC) else None
+    return BIN if all(os.path.exists(b) for b in bins) else None
 
 
-def run(mesh, order: int, c0: np.ndarray, t_end: float, timeout: float = 900.0) -> dict:
+def run(mesh, order: int, c0: np.ndarray, t_end: float, timeout: float = 900.0, problem: str | None = None,
+        rk2: bool = False) -> dict:
     """Advance the Euler state c0 (layout c[4][Np][E], FP64) on `mesh` (a
-    dgcuda_gb300.mesh.Mesh, periodic) to t_end with the reference's solver."""
-    return _run(BIN, mesh, order, c0, 4, 0, t_end, timeout)
+    dgcuda_gb300.mesh.Mesh) to t_end with the reference's solver: periodic
+    meshes with problem None, else boundary sides with the hooks of the
+    reference's "cylinder" or "supersonic" problem file; RK4, or RK2 with rk2."""
+    binary = BIN if problem is None else BIN_PROBLEM[problem]
+    return _run(binary, mesh, order, c0, 4, 0, t_end, timeout, int(bool(rk2)))
 
 
 def run_advection(mesh, order: int, c0: np.ndarray, dt: float, steps: int, timeout: float = 900.0) -> dict:
     """`steps` RK4 steps of dt of the advection state c0 (c[Np][E], FP64) on
     `mesh` (periodic) with the reference's advection solver (a = (1,1))."""
-    return _run(BIN_ADVEC, mesh, order, c0, 1, int(steps), dt, timeout)
+    return _run(BIN_ADVEC, mesh, order, c0, 1, int(steps), dt, timeout, 0)
 
 
-def _run(binary, mesh, order, c0, nv, steps, t_in, timeout):
+def _run(binary, mesh, order, c0, nv, steps, t_in, timeout, rk2):
     if build() is None:
         raise RuntimeError("the reference's CUDA solvers are not built (no reference sources)")
     binp = binary
@@ -61,7 +72,7 @@ def _run(binary, mesh, order, c0, nv, steps, t_in, timeout):
     with tempfile.TemporaryDirectory() as td:
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
-            f.write(struct.pack("<4i", E, S, order, steps))
+            f.write(struct.pack("<6i", E, S, order, steps, rk2, 0))
             f.write(struct.pack("<d", float(t_in)))
             for a in mesh.vertices():
                 f.write(np.ascontiguousarray(a, dtype="<f8").tobytes())

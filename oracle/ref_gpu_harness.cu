@@ -32,8 +32,9 @@
 // printf is routed to a counter: the Euler time loop prints "\rt = ..." once
 // per step, which gives the number of steps taken.
 //
-// Usage: ref_gpu_euler|ref_gpu_advec <in.bin> <out.bin>
-//   in:  int32 E, S, p, steps; double t (Euler: end time; advection: dt);
+// Usage: ref_gpu_euler|ref_gpu_cylinder|ref_gpu_supersonic|ref_gpu_advec <in.bin> <out.bin>
+//   in:  int32 E, S, p, steps, rk2 (Euler: 1 runs time_integrate_rk2), 0;
+//        double t (Euler: end time; advection: dt);
 //        double V[6][E] (V1x V1y V2x V2y V3x V3y); int32 elem_s[3][E];
 //        int32 sides[4][S] (left_elem right_elem left_side right_side);
 //        double c[NV][Np][E] (NV = 4 Euler, 1 advection)
@@ -65,10 +66,23 @@ static int ref_printf(const char *fmt, ...) {
     return 0;
 }
 
+#ifndef REF_PROBLEM
+#define REF_PROBLEM 0
+#endif
 #define printf ref_printf
 #define __syncthreads() ((void)0)
 #if REF_ADVECTION
 #include "2dadvec/2dadvec.cu"
+#elif REF_PROBLEM == 1
+// the reference's cylinder problem file, its own hooks (its main renamed)
+#define main ref_problem_main
+#include "conservation/euler/cylinder/cylinder.cu"
+#undef main
+#elif REF_PROBLEM == 2
+// the reference's supersonic-vortex problem file, its own hooks
+#define main ref_problem_main
+#include "conservation/euler/supersonic/supersonic.cu"
+#undef main
 #else
 #include "conservation/euler/euler.cu"
 #endif
@@ -79,6 +93,8 @@ static int ref_printf(const char *fmt, ...) {
 constexpr int kVars = 1;
 #else
 constexpr int kVars = 4;
+#endif
+#if !REF_ADVECTION && REF_PROBLEM == 0
 // ---- the problem: periodic meshes only, gamma 1.4 -------------------------
 int limiter = NO_LIMITER;
 int time_integrator = RK4;
@@ -138,14 +154,15 @@ int main(int argc, char **argv) {
     }
     FILE *fi = std::fopen(argv[1], "rb");
     if (!fi) { std::fprintf(stderr, "cannot open %s\n", argv[1]); return 2; }
-    int hdr[4];
+    int hdr[6];
     double t_in = 0.0;   // Euler: end time; advection: dt
-    if (std::fread(hdr, sizeof(int), 4, fi) != 4 || std::fread(&t_in, sizeof(double), 1, fi) != 1) {
+    if (std::fread(hdr, sizeof(int), 6, fi) != 6 || std::fread(&t_in, sizeof(double), 1, fi) != 1) {
         std::fprintf(stderr, "bad header\n");
         return 2;
     }
-    const int num_elem = hdr[0], num_sides = hdr[1], n = hdr[2], timesteps = hdr[3];
-    if (num_elem <= 0 || num_sides <= 0 || n < 0 || n > 5 || !(t_in > 0.0) || (REF_ADVECTION && timesteps < 1)) {
+    const int num_elem = hdr[0], num_sides = hdr[1], n = hdr[2], timesteps = hdr[3], use_rk2 = hdr[4];
+    if (num_elem <= 0 || num_sides <= 0 || n < 0 || n > 5 || !(t_in > 0.0) || (REF_ADVECTION && timesteps < 1) ||
+        use_rk2 < 0 || use_rk2 > 1 || (REF_ADVECTION && use_rk2)) {
         std::fprintf(stderr, "bad sizes\n");
         return 2;
     }
@@ -161,8 +178,10 @@ int main(int argc, char **argv) {
     std::fclose(fi);
     for (size_t s = 0; s < S; ++s) {
         const int L = sd[s], R = sd[S + s], ls = sd[2 * S + s], rs = sd[3 * S + s];
-        if (L < 0 || L >= num_elem || R < 0 || R >= num_elem || ls < 0 || ls > 2 || rs < 0 || rs > 2) {
-            std::fprintf(stderr, "side %zu: the harness takes periodic meshes only\n", s);
+        // boundary sides (-1 reflecting, -2 outflow, -3 inflow) only with a problem file's hooks
+        const bool bnd_ok = !REF_ADVECTION && REF_PROBLEM != 0 && R >= -3 && R <= -1;
+        if (L < 0 || L >= num_elem || ls < 0 || ls > 2 || ((R < 0 || R >= num_elem || rs < 0 || rs > 2) && !bnd_ok)) {
+            std::fprintf(stderr, "side %zu: the harness takes periodic meshes only, or boundary sides with a problem file\n", s);
             return 2;
         }
     }
@@ -186,6 +205,11 @@ int main(int argc, char **argv) {
 
     // the reference driver's set-up (Euler: conservation/main.cu:68-163;
     // advection: src/2d/main.cu:101-186)
+#if !REF_ADVECTION
+    // the integrator the problem file would pick, chosen here (init_gpu sizes
+    // its stage buffers by it, conserv.cu:238-253)
+    time_integrator = use_rk2 ? RK2 : RK4;
+#endif
     init_gpu(num_elem, num_sides, n_p, V1x, V1y, V2x, V2y, V3x, V3y, left_side_number, right_side_number,
              sx1.data(), sy1.data(), sx2.data(), sy2.data(), elem_s1, elem_s2, elem_s3, left_elem, right_elem);
     checkCudaError("error after gpu init.");
@@ -238,7 +262,10 @@ int main(int argc, char **argv) {
     time_integrate_rk4(t_in, n_quad, n_quad1d, n_p, n, num_elem, num_sides, 0, 0, timesteps);
     g_steps = timesteps;
 #else
-    time_integrate_rk4(n_quad, n_quad1d, n_p, n, num_elem, num_sides, t_in, min_r);
+    if (use_rk2)
+        time_integrate_rk2(n_quad, n_quad1d, n_p, n, num_elem, num_sides, t_in, min_r);
+    else
+        time_integrate_rk4(n_quad, n_quad1d, n_p, n, num_elem, num_sides, t_in, min_r);
 #endif
     cudaDeviceSynchronize();
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

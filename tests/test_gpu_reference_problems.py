@@ -1,0 +1,102 @@
+"""Boundary sides and the reference's problem plug-ins pinned to the
+reference's own CUDA solver on its own meshes.
+
+oracle/ref_gpu_harness.cu is compiled with the reference's cylinder and
+supersonic-vortex problem files (src/2d/conservation/euler/cylinder/
+cylinder.cu, euler/supersonic/supersonic.cu), whose hooks give the ghost states
+of reflecting (-1), outflow (-2) and inflow (-3) sides (dispatched by
+eval_left_right, src/2d/conservation/conserv_kernels.cu:657-679).  The meshes
+are the reference's cylinder.pmsh and sv1.pmsh (tests/golden/
+reference_meshes.npz).  Both sides start from the same FP64 coefficients and
+advance to the same end time with the reference's CFL rule, with
+time_integrate_rk2 (the cylinder problem's integrator, cylinder.cu:13,
+time_integrator.cu:466-614) or time_integrate_rk4 (the supersonic problem's).
+
+The reference's hooks take square roots and powers in FP32 (sqrtf of the
+radius in the radial reflections, powf in the supersonic state); the GPU path
+does so with DGX_OPT_HOOK_MATH = DGX_HOOK_MATH_REFERENCE.  Tolerances
+(relative L2 per conserved variable):
+  FP64 path (reference hook arithmetic) vs the reference   <= 1e-9
+  FP64 path (FP64 hook arithmetic) vs the reference        <= 1e-6
+  FP32 path vs the reference                               <= 1e-5
+"""
+import os
+
+import numpy as np
+import pytest
+
+from dgcuda_gb300 import _ffi
+from dgcuda_gb300.mesh import read_pmsh
+from dgcuda_gb300.solver import Solver
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_meshes.npz")
+CYLINDER = (0.38,)          # MACH of cylinder.cu:11
+SUPERSONIC = (2.25, 1.0125)  # MACH and the density constant of supersonic.cu:11,30
+
+
+@pytest.fixture(scope="module")
+def ref_gpu():
+    from oracle import ref_gpu
+    if ref_gpu.build() is None:
+        pytest.skip("the reference's CUDA sources are not at hand (make -C oracle ref-src)")
+    return ref_gpu
+
+
+def reference_mesh(name, tmp_path_factory):
+    z = np.load(GOLDEN)
+    p = tmp_path_factory.mktemp("meshes") / f"{name}.pmsh"
+    p.write_bytes(z[f"{name}_pmsh"].tobytes())
+    return read_pmsh(str(p))
+
+
+def rel_l2(a, b):
+    a = a.reshape(4, -1)
+    b = b.reshape(4, -1)
+    return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+
+
+CASES = [
+    # (mesh, problem, initial-condition id, params, order, RK2?, CFL steps to the end time)
+    ("cylinder", "cylinder", _ffi.IC_CYLINDER, CYLINDER, 1, True, 40.5),
+    ("cylinder", "cylinder", _ffi.IC_CYLINDER, CYLINDER, 2, True, 30.5),
+    ("cylinder", "cylinder", _ffi.IC_CYLINDER, CYLINDER, 2, False, 20.5),
+    ("sv1", "supersonic", _ffi.IC_SUPERSONIC_VORTEX, SUPERSONIC, 1, False, 40.5),
+    ("sv1", "supersonic", _ffi.IC_SUPERSONIC_VORTEX, SUPERSONIC, 3, False, 20.5),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[1]}-p{c[4]}-{'rk2' if c[5] else 'rk4'}" for c in CASES])
+def test_problem_matches_reference_solver(case, ref_gpu, gpu, oracle_mod, tmp_path_factory):
+    mesh_name, problem, ic, params, p, rk2, nsteps = case
+    orc = oracle_mod
+    m = reference_mesh(mesh_name, tmp_path_factory)
+    m.check()
+    o = orc.Oracle(m, p, orc.EULER, orc.LLF)
+    c0 = o.project(ic, params)
+    t_end = nsteps * o.cfl_dt(c0)
+    ref = ref_gpu.run(m, p, c0, t_end, problem=problem, rk2=rk2)
+    integrator = _ffi.RK2 if rk2 else _ffi.RK4
+    errs = {}
+    for precision, hook in ((_ffi.FP64, _ffi.HOOK_MATH_REFERENCE), (_ffi.FP64, _ffi.HOOK_MATH_DOUBLE),
+                            (_ffi.FP32, _ffi.HOOK_MATH_REFERENCE)):
+        sv = Solver(m, p, _ffi.EULER, _ffi.FLUX_LLF, precision, integrator=integrator)
+        sv.set_boundary(_ffi.BC_PROBLEM, ic, params)
+        sv.set_option(_ffi.OPT_STAGE_TIME, _ffi.STAGE_TIME_REFERENCE)
+        sv.set_option(_ffi.OPT_HOOK_MATH, hook)
+        sv.set_state(c0)
+        sv.set_dt(None, cfl=0.7)
+        n, t = sv.run(t_end=t_end)
+        assert n == ref["steps"], (n, ref["steps"])
+        assert abs(t - t_end) <= 1e-12 * t_end
+        errs[(precision, hook)] = rel_l2(sv.get_state(), ref["state"])
+        sv.close()
+    print(f"{problem} p={p} {'rk2' if rk2 else 'rk4'} steps={ref['steps']}: "
+          + ", ".join(f"{'fp64' if k[0] == _ffi.FP64 else 'fp32'}/"
+                      f"{'ref' if k[1] == _ffi.HOOK_MATH_REFERENCE else 'double'} {v.max():.2e}"
+                      for k, v in errs.items()))
+    assert errs[(_ffi.FP64, _ffi.HOOK_MATH_REFERENCE)].max() <= 1e-9, errs
+    assert errs[(_ffi.FP64, _ffi.HOOK_MATH_DOUBLE)].max() <= 1e-6, errs
+    assert errs[(_ffi.FP32, _ffi.HOOK_MATH_REFERENCE)].max() <= 1e-5, errs
