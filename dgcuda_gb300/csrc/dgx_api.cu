@@ -179,14 +179,10 @@ int run_stage_raw(dgx_solver *sv, int stage, cudaStream_t st) {
         if (!rc) sv->launches++;
         return rc;
     }
-    switch (stage) {
-    case 0:
-        return stage_launch(sv, 1, s.c, s.c, s.acc, s.ua, 0.0, 0.0, st);
-    case 1: return stage_launch(sv, 2, s.ua, s.c, s.acc, s.ub, 0.0, 0.0, st);
-    case 2: return stage_launch(sv, 3, s.ub, s.c, s.acc, s.ua, 0.0, 0.0, st);
-    case 3: return stage_launch(sv, 4, s.ua, s.c, s.acc, s.c, 0.0, 0.0, st);
-    default: set_error("stage must be 0..3"); return DGX_ERR_INVALID;
-    }
+    const StageArgs a = rk4_stage_args(sv, stage);
+    rc = launch_stage(s.precision, s.order, s.equation, a, st);
+    if (!rc) sv->launches++;
+    return rc;
 }
 
 int write_scalar(SolverDev &s, int idx, double v) {
@@ -253,6 +249,34 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
         a.geo = m.geo32;
         a.fn = m.fn32;
     }
+    a.aux = nullptr;
+    a.rk13 = 0;
+    return a;
+}
+
+// Classic RK4 (time_integrator.cu:194-218) over the buffers c (state), ua, ub
+// (stage inputs) and acc.  The reference keeps k1..k4; the 16-pass fused form
+// keeps acc = c + k1/6 (+ k2/3 + k3/3) written by every stage.  The 13-pass
+// form writes the accumulator once: with u2 = c + k1/2 and u3 = c + k2/2,
+//   c + k1/6 + k2/3 + k3/3 = c + ((u2 - c) + 2 (u3 - c) + k3) / 3,
+// so stage 1 reads c and writes u2 (2 passes), stage 2 reads u2 and c and
+// writes u3 (3), stage 3 reads u3, c and u2 and writes u4 = c + k3 over u2 and
+// the accumulator (5), stage 4 reads u4 and the accumulator and writes c (3).
+// The differences u2 - c, u3 - c are exact (Sterbenz) for steps that change a
+// coefficient by less than half its value, so the accumulator's rounding is
+// of the order of the 16-pass form's.
+StageArgs rk4_stage_args(dgx_solver *sv, int stage) {
+    SolverDev &s = sv->s;
+    const bool rk13 = !s.limiter;
+    StageArgs a;
+    switch (stage) {
+    case 0: a = make_stage_args(sv, 1, s.c, s.c, s.acc, s.ua, 0.0, 0.0); break;
+    case 1: a = make_stage_args(sv, 2, s.ua, s.c, s.acc, s.ub, 0.0, 0.0); break;
+    case 2: a = make_stage_args(sv, 3, s.ub, s.c, s.acc, s.ua, 0.0, 0.0); break;
+    default: a = make_stage_args(sv, 4, s.ua, s.c, s.acc, s.c, 0.0, 0.0); break;
+    }
+    a.rk13 = rk13 ? 1 : 0;
+    if (rk13 && stage == 2) a.aux = s.ua;   // u2, overwritten in place by u4
     return a;
 }
 

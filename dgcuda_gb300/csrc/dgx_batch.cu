@@ -108,12 +108,7 @@ int class_host_args(dgx_batch *b, BatchClass &k, std::vector<StageArgs> &host) {
             const int saved = s.prefetch;
             s.prefetch = k.prefetch;
             StageArgs &h = host[stage * ns + j];
-            switch (stage) {
-            case 0: h = make_stage_args(sv, 1, s.c, s.c, s.acc, s.ua, 0.0, 0.0); break;
-            case 1: h = make_stage_args(sv, 2, s.ua, s.c, s.acc, s.ub, 0.0, 0.0); break;
-            case 2: h = make_stage_args(sv, 3, s.ub, s.c, s.acc, s.ua, 0.0, 0.0); break;
-            default: h = make_stage_args(sv, 4, s.ua, s.c, s.acc, s.c, 0.0, 0.0); break;
-            }
+            h = rk4_stage_args(sv, stage);
             s.prefetch = saved;
             nslot = std::max(nslot, h.nslot);
             plane = std::max(plane, h.prefetch);

@@ -217,6 +217,14 @@ struct StageArgs {
     const void *c;     // base state
     void *acc;         // accumulator
     void *out;         // k (mode 0), next stage input (1..3), state (4)
+    // RK4 in 13 state passes per step (rk13 = 1): stage 1 writes only u2, stage
+    // 2 only u3, and stage 3 forms the accumulator c + k1/6 + k2/3 + k3/3 from
+    // u2 = c + k1/2 (aux, read before `out` overwrites it in place) and its own
+    // input u3 = c + k2/2; rk13 = 0: the 16-pass form with the accumulator
+    // written by every stage (kept for the per-stage limiter, which changes the
+    // stage states after they are written)
+    const void *aux;
+    int rk13;
     const int *nbr;
     const int *halo_off;
     const int *halo_list;
@@ -297,6 +305,9 @@ int launch_batch_dt(const DtArgs *args, const int2 *items, int n_items, cudaStre
 // per-solve stage arguments (dgx_api.cu)
 StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c, void *acc,
                           void *out, double dt, double t);
+// the arguments of RK4 stage 0..3 on the solver's resident buffers (the
+// 13-pass form unless the per-stage limiter is on)
+StageArgs rk4_stage_args(dgx_solver *sv, int stage);
 
 // Creation of meshes and solvers with their device memory from `pool`
 // (nullptr: cudaMalloc), uploads and initialisation on `st`.  Without `async`,

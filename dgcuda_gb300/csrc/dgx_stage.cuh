@@ -363,7 +363,11 @@ __device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, uns
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         const int cnt = min(kTile, E - tile * kTile);
         const int nplanes = NV * NP;
-        const int ncopy = (a.mode == 4) ? nplanes : 2 * nplanes;
+        // mode 2 and 3: the base state, then the accumulator (13-pass RK4: mode
+        // 2 the base state alone, mode 3 the base state and u2); mode 4: the
+        // accumulator
+        const bool base_only = a.rk13 && a.mode == 2;
+        const int ncopy = (a.mode == 4 || base_only) ? nplanes : 2 * nplanes;
         // plane pl's slice [g0, g0 + cnt) widened to [g0 & -A, (g0 + cnt + A-1) & -A)
         // (the state buffers carry 16 bytes of slack past their end)
         const size_t A = kPreAlign;
@@ -377,13 +381,15 @@ __device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, uns
         }
         __syncwarp();
         for (int q = tid; q < ncopy; q += 32) {
-            // planes [0, nplanes): base state (modes 2, 3), then the accumulator;
-            // mode 4 copies only the accumulator, to planes [0, nplanes)
+            // planes [0, nplanes): base state (modes 2, 3), then the accumulator
+            // (13-pass mode 3: u2); mode 4 copies only the accumulator, to
+            // planes [0, nplanes)
             const int which = (a.mode == 4) ? 1 : (q >= nplanes);
             const int pl = q % nplanes;
             const size_t g0 = pl * SE + static_cast<size_t>(tile) * kTile;
             const size_t a0 = g0 & ~(A - 1), a1 = (g0 + cnt + A - 1) & ~(A - 1);
-            const R *src = static_cast<const R *>(which ? a.acc : a.c) + a0;
+            const void *second = (a.rk13 && a.mode == 3) ? a.aux : static_cast<const void *>(a.acc);
+            const R *src = static_cast<const R *>(which ? second : a.c) + a0;
             bulk_copy_g2s(s_pre + static_cast<size_t>(q) * a.prefetch, src, static_cast<unsigned>((a1 - a0) * sizeof(R)),
                           bar);
         }
@@ -400,7 +406,10 @@ struct IntC {
 // Mass inverse and the RK combination of the stage (time_integrator.cu:194-218,
 // 445-464, 622-700): k = dt/J rhs, then per mode of the kernel
 //   0 k;  1 u2 = c + k/2, acc = c + k/6;  2/3 u = c + alpha k, acc += k/3;
-//   4 c = acc + k/6;  5 out = u + alpha k;  6 out = c + alpha k.
+//   4 c = acc + k/6;  5 out = u + alpha k;  6 out = c + alpha k;
+// in the 13-pass RK4 form (a.rk13, see rk4_stage_args) modes 1 and 2 write no
+// accumulator and mode 3 forms it, acc = c + ((u2 - c) + 2 (u3 - c) + k3)/3,
+// with u3 this stage's input (the `c` argument) and u2 from a.aux.
 // Writes the variables V0 .. V0+VC-1 (all of them by default; rhs and c hold
 // just those).  Waits (bounded) for the tile's prefetched base state and
 // accumulator when `pre`; `row` is the element's index in the tile; returns
@@ -431,10 +440,12 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
     // kTile-value planes (E a multiple of kPreAlign), at compile-time offsets.
     auto rk_tail = [&](auto kind) {
         constexpr int K = decltype(kind)::value;
+        // the second operand: the accumulator, or u2 in mode 3 of the 13-pass form
+        const bool from_u2 = a.rk13 && a.mode == 3;
         const R *pc, *pacc;
         if constexpr (K == 0) {
             pc = static_cast<const R *>(a.c) + e;
-            pacc = static_cast<const R *>(a.acc) + e;
+            pacc = static_cast<const R *>(from_u2 ? a.aux : static_cast<const void *>(a.acc)) + e;
         } else {
             pc = s_pre + row;
             pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * a.prefetch) + row;
@@ -453,6 +464,40 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
                     const int pi = (V0 + n) * NP + i;
                     oe[pi * SE] = fma(R(1.0 / 6.0), sc * rhs[n][i], at(pacc, pi));
                 }
+        } else if (a.rk13) {
+            // 2: u3 = c + k2/2;  3: u4 = c + k3 (over u2) and
+            //    acc = c + ((u2 - c) + 2 (u3 - c) + k3) / 3, u3 the stage's input
+            const R alpha = a.mode == 2 ? R(0.5) : R(1);
+            R *__restrict__ ae = static_cast<R *>(a.acc) + e;
+            if (a.mode == 3) {
+                // without the prefetch u2 is read where u4 goes: all of the
+                // element's u2 values are read before its first write
+                R u2v[VC][NP];
+#pragma unroll
+                for (int n = 0; n < VC; ++n)
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) u2v[n][i] = at(pacc, (V0 + n) * NP + i);
+                R *o3 = static_cast<R *>(a.out) + e;
+#pragma unroll
+                for (int n = 0; n < VC; ++n)
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) {
+                        const R kk = sc * rhs[n][i];
+                        const int pi = (V0 + n) * NP + i;
+                        const R base = at(pc, pi);
+                        const R dsum = fma(R(2), c[n][i] - base, u2v[n][i] - base) + kk;
+                        ae[pi * SE] = fma(R(1.0 / 3.0), dsum, base);
+                        o3[pi * SE] = fma(alpha, kk, base);
+                    }
+            } else {
+#pragma unroll
+                for (int n = 0; n < VC; ++n)
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) {
+                        const int pi = (V0 + n) * NP + i;
+                        oe[pi * SE] = fma(alpha, sc * rhs[n][i], at(pc, pi));
+                    }
+            }
         } else {             // 2: u3 = c + k2/2, acc += k2/3;  3: u4 = c + k3, acc += k3/3
             R *__restrict__ ae = static_cast<R *>(a.acc) + e;
             const R alpha = a.mode == 2 ? R(0.5) : R(1);
@@ -474,8 +519,16 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
 #pragma unroll
             for (int i = 0; i < NP; ++i) out[((V0 + n) * NP + i) * SE + e] = sc * rhs[n][i];
         break;
-    case 1: {   // u2 = c + k1/2, acc = c + k1/6
+    case 1: {   // u2 = c + k1/2, and in the 16-pass form acc = c + k1/6
         R *__restrict__ ae = static_cast<R *>(a.acc) + e;
+        if (a.rk13) {
+#pragma unroll
+            for (int n = 0; n < VC; ++n)
+#pragma unroll
+                for (int i = 0; i < NP; ++i)
+                    oe[((V0 + n) * NP + i) * SE] = fma(R(0.5), sc * rhs[n][i], c[n][i]);
+            break;
+        }
 #pragma unroll
         for (int n = 0; n < VC; ++n)
 #pragma unroll
