@@ -1,5 +1,6 @@
-/* dgx_drop_in.c -- the reference-side binding of INTEGRATION.md as a plain C
- * program (test infrastructure: built and run by tests/test_gpu_c_driver.py).
+/* dgx_drop_in.c -- the reference-side binding of the library, as a driver of
+ * the reference would add it, written as a plain C program (test
+ * infrastructure: built and run by tests/test_gpu_c_driver.py).
  *
  * It does what the reference's run_dgcuda does around its time loop
  * (src/2d/conservation/main.cu:54-209) with the library in place of init_gpu's
@@ -51,7 +52,7 @@ int main(int argc, char **argv) {
     CHECK(dgx_pmsh_read(mesh_path, V, es, sides));
     const size_t E = (size_t)num_elem, S = (size_t)num_sides;
 
-    /* the binding of INTEGRATION.md */
+    /* the binding: mesh, solver, initial state, time loop, state out */
     dgx_mesh *mesh;
     dgx_solver *solver;
     dgx_solver_desc desc = {.order = order, .equation = DGX_EULER, .flux = DGX_FLUX_LLF,

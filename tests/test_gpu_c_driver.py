@@ -1,5 +1,5 @@
-"""The drop-in binding compiled from C: tests/c_driver/dgx_drop_in.c follows
-INTEGRATION.md's reference-side snippet (dgx_pmsh_read, dgx_mesh_create,
+"""The drop-in binding compiled from C: tests/c_driver/dgx_drop_in.c makes the
+calls a reference driver makes (dgx_pmsh_read, dgx_mesh_create,
 dgx_solver_create, dgx_solver_set_boundary, dgx_project_ic, dgx_set_dt,
 dgx_run, dgx_get_state) against include/dgx.h and libdgx.so, with gcc, and
 runs the reference's cylinder problem on the reference's own cylinder.pmsh.
