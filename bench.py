@@ -526,7 +526,8 @@ def _serve_window(specs, rate, arrive_s, serve_s, keep=()):
     return rec, kept
 
 
-def run_served_stated(rates=(50, 200, 1000, 2000), arrive_s=6.0, serve_s=12.0, capacity_s=20.0, plain_s=15.0):
+def run_served_stated(rates=(50, 200, 1000, 2000), arrive_s=6.0, serve_s=12.0, capacity_s=20.0, plain_s=15.0,
+                      subset=96):
     """Served configuration at its stated sizes: the 10,000-request stream of
     _served_stream (N up to 512, end times up to a full flow-through).  Its
     work (~1e13 DOF-updates, hours of GPU time) cannot finish in a benchmark,
@@ -539,15 +540,17 @@ def run_served_stated(rates=(50, 200, 1000, 2000), arrive_s=6.0, serve_s=12.0, c
       * capacity: the stream submitted at once, served for capacity_s seconds;
       * plain: the same stream solved one by one with the public single-solve
         calls for plain_s seconds (requests that start are run to their end);
-      * accuracy: relative L2 per variable of finished requests (the first
-        requests of the stream with N <= 64) against the same request solved in
-        FP64 on the GPU (the FP64 path, held to 1e-11 of the CPU oracle by the
-        parity tests)."""
+      * same requests: the stream's first `subset` requests with N <= 128,
+        served (submitted at once, run to the last one's end) and solved one by
+        one on the plain path, each to its full end time, so both paths do the
+        same work;
+      * accuracy: relative L2 per variable of the first 8 of those requests
+        against the same request solved in FP64 on the GPU (the FP64 path, held
+        to 1e-11 of the CPU oracle by the parity tests)."""
     import torch
     from dgcuda_gb300 import _ffi
     from dgcuda_gb300.solver import DeviceMesh, Solver
     specs = _served_stream()
-    keep = [k for k, sp in enumerate(specs[:200]) if sp["n"] <= 64][:8]
     out = {"workload": "10,000 requests: N log-uniform [16,512], p 1..4, equations 50/50, end times U[0.1,1] "
                        "flow-through, Poisson arrivals, 150 GB admission budget (time-boxed prefixes)",
            "stream_requests": len(specs), "rates": []}
@@ -556,7 +559,7 @@ def run_served_stated(rates=(50, 200, 1000, 2000), arrive_s=6.0, serve_s=12.0, c
         rec["rate_req_s"] = rate
         rec["window"] = f"arrivals for {arrive_s:g} s, served until {serve_s:g} s"
         out["rates"].append(rec)
-    cap, kept = _serve_window(specs, 0, 0.0, capacity_s, keep=keep)
+    cap, _ = _serve_window(specs, 0, 0.0, capacity_s)
     cap["window"] = f"the stream submitted at once, served for {capacity_s:g} s"
     out["capacity"] = cap
     # the plain path: one request after another through the single-solve calls
@@ -574,9 +577,27 @@ def run_served_stated(rates=(50, 200, 1000, 2000), arrive_s=6.0, serve_s=12.0, c
     out["plain"] = {"value": dof / plain_wall, "requests": done, "wall_s": plain_wall,
                     "path": "dgx_mesh_create_periodic_square + dgx_solver_create + dgx_project_ic + dgx_run per request"}
     out["capacity_vs_plain"] = cap["value"] / out["plain"]["value"] if out["plain"]["value"] else None
+    # the same requests through both paths, each to its end time
+    sel = [k for k, sp in enumerate(specs) if sp["n"] <= 128][:subset]
+    sub = [specs[k] for k in sel]
+    srv_rec, kept = _serve_window(sub, 0, 0.0, 600.0, keep=range(8))
+    t0, pdof = time.perf_counter(), 0.0
+    for sp in sub:
+        sv = _native_solver(sp)
+        n, _ = sv.run(t_end=sp["t_end"])
+        pdof += n * sv.nv * sv.np * sv.E
+        sv.close()
+    torch.cuda.synchronize()
+    pwall = time.perf_counter() - t0
+    out["same_requests"] = {
+        "requests": f"the stream's first {len(sub)} requests with N <= 128 (full end times)",
+        "served": {"wall_s": srv_rec["wall_s"], "value": srv_rec["dof_updates"] / srv_rec["wall_s"],
+                   "completed": srv_rec["completed"], "p50_s": srv_rec["p50_s"], "p99_s": srv_rec["p99_s"]},
+        "plain": {"wall_s": pwall, "value": pdof / pwall},
+        "served_vs_plain": (srv_rec["dof_updates"] / srv_rec["wall_s"]) / (pdof / pwall) if pdof else None}
     rows, worst = [], [0.0] * 4
     for k, (c, steps, t) in kept.items():
-        sp = specs[k]
+        sp = sub[k]
         dm = DeviceMesh.periodic_square(sp["n"], sp["lx"], sp["ly"], sp["jitter"], sp["seed"])
         ref = Solver(dm, sp["order"], sp["equation"], _ffi.FLUX_LLF, _ffi.FP64, 1.4)
         ref.project(sp["ic"], sp["params"])
@@ -587,7 +608,7 @@ def run_served_stated(rates=(50, 200, 1000, 2000), arrive_s=6.0, serve_s=12.0, c
         err = [float(np.linalg.norm(c[n] - b[n]) / np.linalg.norm(b[n])) for n in range(c.shape[0])]
         for n, v in enumerate(err):
             worst[n] = max(worst[n], v)
-        rows.append({"request": k, "n": sp["n"], "order": sp["order"], "steps": steps,
+        rows.append({"request": sel[k], "n": sp["n"], "order": sp["order"], "steps": steps,
                      "equation": "euler" if sp["equation"] == _ffi.EULER else "advection", "rel_l2": err})
     out["accuracy"] = {"reference": "the same request in FP64 on the GPU, to the same end time",
                        "max_rel_l2_per_variable": worst, "max_rel_l2": max(worst) if rows else None,

@@ -801,8 +801,9 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
                 R2 hra[2], hsa[2], hrb[2], hsb[2];
                 metric(Ua, hra, hsa);
                 metric(Ub, hrb, hsb);
+                // mode 0 is constant: its weighted gradients are 0
 #pragma unroll
-                for (int i = 0; i < NP; ++i) {
+                for (int i = 1; i < NP; ++i) {
                     const R2 tx = *reinterpret_cast<const R2 *>(&c_tab[L::GX + i * NQ + q]);
                     const R2 ty = *reinterpret_cast<const R2 *>(&c_tab[L::GY + i * NQ + q]);
 #pragma unroll
@@ -832,7 +833,7 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
 #pragma unroll
                 for (int h = 0; h < 2; ++h)
 #pragma unroll
-                    for (int i = 0; i < NP; ++i)
+                    for (int i = 1; i < NP; ++i)   // mode 0: gradients 0
                         rhs2[h][i] = fma2(dup2(c_tab[L::GX + i * NQ + q]), hr2[h],
                                           fma2(dup2(c_tab[L::GY + i * NQ + q]), hs2[h], rhs2[h][i]));
             }
@@ -884,16 +885,21 @@ __device__ __forceinline__ bool stage_tile_pair(const StageArgs &a, const int ti
             Fh2[j][0] = mk2(Fh[0], Fh[1]);
             Fh2[j][1] = mk2(Fh[2], Fh[3]);
         }
+        // the fluxes scaled by -len/2 first, then lifted straight into the
+        // modes (each element scales its own, exactly negated, flux: the two
+        // elements of a side still get contributions of equal magnitude)
         const R2 sg2 = dup2(-hl);
+#pragma unroll
+        for (int j = 0; j < NQ1; ++j)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) Fh2[j][h] = fmul2(sg2, Fh2[j][h]);
 #pragma unroll
         for (int h = 0; h < 2; ++h)
 #pragma unroll
-            for (int i = 0; i < NP; ++i) {
-                R2 s2 = mk2(R(0), R(0));
+            for (int i = 0; i < NP; ++i)
 #pragma unroll
-                for (int j = 0; j < NQ1; ++j) s2 = fma2(dup2(c_tab[L::LIFT + (k * NP + i) * NQ1 + j]), Fh2[j][h], s2);
-                rhs2[h][i] = fma2(sg2, s2, rhs2[h][i]);
-            }
+                for (int j = 0; j < NQ1; ++j)
+                    rhs2[h][i] = fma2(dup2(c_tab[L::LIFT + (k * NP + i) * NQ1 + j]), Fh2[j][h], rhs2[h][i]);
     }
 
     R rhs[NV][NP], c[NV][NP];
@@ -1261,7 +1267,7 @@ __device__ __forceinline__ bool stage_tile(const StageArgs &a, const int tile, u
                 const R hr = fx[n] * ys - fy[n] * xs;
                 const R hs = fy[n] * xr - fx[n] * yr;
 #pragma unroll
-                for (int i = 0; i < NP; ++i)
+                for (int i = 1; i < NP; ++i)   // mode 0 is constant: its weighted gradients are 0
                     rhs[n][i] = fma(c_tab[L::GX + i * NQ + q], hr, fma(c_tab[L::GY + i * NQ + q], hs, rhs[n][i]));
             }
         }
