@@ -34,6 +34,8 @@ struct BatchClass {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     long long dofs = 0;
+    std::vector<StageArgs> h_args;           // host copy of d_args (stage-major), for the parameter launches
+    std::vector<int> tiles;                  // tiles of each solve
 };
 
 // elements per work item of the batched CFL kernel (8 per thread)
@@ -80,6 +82,30 @@ namespace dgx {
 namespace {
 
 int class_launch(dgx_batch *b, BatchClass &k, int stage, cudaStream_t st) {
+    if (k.persistent == 0) {
+        // the flat grid: the solves' arguments as kernel parameters, up to
+        // kParamSolves solves per launch
+        const size_t ns = k.solves.size();
+        static thread_local BatchParamArgs p;
+        p.nslot = k.nslot;
+        p.prefetch = (stage >= 1 && k.prefetch) ? k.pre_plane : 0;
+        p.bnd = k.bnd;
+        for (size_t j0 = 0; j0 < ns; j0 += kParamSolves) {
+            const int n = static_cast<int>(std::min<size_t>(kParamSolves, ns - j0));
+            int t = 0;
+            for (int j = 0; j < n; ++j) {
+                p.args[j] = k.h_args[stage * ns + j0 + j];
+                p.tile_start[j] = t;
+                t += k.tiles[j0 + j];
+            }
+            p.tile_start[n] = t;
+            p.n = n;
+            const int rc = launch_batch_param(k.precision, k.order, k.equation, p, t, st);
+            if (rc) return rc;
+            if (t > 0) b->launches++;
+        }
+        return DGX_OK;
+    }
     BatchStageArgs a;
     a.args = k.d_args[stage];
     a.items = k.d_items;
@@ -129,7 +155,14 @@ int class_host_args(dgx_batch *b, BatchClass &k, std::vector<StageArgs> &host) {
 // set the class kernel's shared-memory limit outside any capture (grid 0: no launch)
 int class_configure(BatchClass &k) {
     BatchStageArgs probe{k.d_args[1], k.d_items, 0, 0, k.nslot, k.prefetch ? k.pre_plane : 0, k.bnd};
-    return launch_batch_stage(k.precision, k.order, k.equation, probe, nullptr);
+    int rc = launch_batch_stage(k.precision, k.order, k.equation, probe, nullptr);
+    if (rc) return rc;
+    static thread_local BatchParamArgs pp;
+    pp.n = 0;
+    pp.nslot = k.nslot;
+    pp.prefetch = k.prefetch ? k.pre_plane : 0;
+    pp.bnd = k.bnd;
+    return launch_batch_param(k.precision, k.order, k.equation, pp, 0, nullptr);
 }
 
 // Upload the per-solve stage arguments of one class for its current options
@@ -139,6 +172,7 @@ int class_upload(dgx_batch *b, BatchClass &k) {
     int rc = class_host_args(b, k, host);
     if (rc) return rc;
     DGX_TRY_CUDA(cudaMemcpy(k.d_args[0], host.data(), host.size() * sizeof(StageArgs), cudaMemcpyHostToDevice));
+    k.h_args = host;
     return class_configure(k);
 }
 
@@ -286,9 +320,11 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
         for (size_t j = 0; j < k.solves.size(); ++j) {
             const int ntiles = b->solvers[k.solves[j]]->mesh->d.num_tiles;
             for (int t = 0; t < ntiles; ++t) items[c].push_back(make_int2(static_cast<int>(j), t));
+            k.tiles.push_back(ntiles);
         }
         k.n_items = static_cast<int>(items[c].size());
         rc = class_host_args(b, k, args[c]);
+        if (!rc) k.h_args = args[c];
     }
     if (rc) { batch_free(b); return rc; }
     // one device block for every array of the batch, filled by one copy

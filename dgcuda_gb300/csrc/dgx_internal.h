@@ -43,6 +43,7 @@ enum StatusBits : unsigned int {
     kStatusNonFinite = 1u,   // NaN/Inf wave speed or state
     kStatusNegative = 2u,    // non-positive density or pressure in a cell average
     kStatusCopyTimeout = 4u, // a bounded wait for an asynchronous copy ran out
+    kStatusBadItem = 8u,     // a batched work item outside its solve's tiles (skipped)
 };
 
 // Elements are processed in tiles of kTile consecutive elements, one CTA per
@@ -258,6 +259,25 @@ struct BatchStageArgs {
     int bnd;                 // any solve of the class has boundary sides
 };
 
+// Batched launch with the solves' arguments in the kernel's parameter space (up
+// to 32 KB of parameters per launch, CUDA 12.1 and later): up to kParamSolves
+// solves of one class; CTA b takes tile b - tile_start[j] of the solve j with
+// tile_start[j] <= b < tile_start[j+1].  The constant bank serves the
+// arguments to every CTA without a dependent global load before its work.
+// The block is kept below 31 KB, with the small tables first: measured on
+// GB300, a runtime-indexed read of the tile offsets placed past the solves'
+// arguments, near the end of a 32 KB parameter block, returned 0.
+constexpr int kParamSolves = 88;
+struct BatchParamArgs {
+    int n;          // solves in this launch
+    int nslot;      // largest nslot of the class (shared-memory size)
+    int prefetch;   // values per prefetched plane of the class (0: none)
+    int bnd;
+    int tile_start[kParamSolves + 1];
+    StageArgs args[kParamSolves];
+};
+static_assert(sizeof(BatchParamArgs) <= 31 * 1024, "kept below 31 KB of the 32,764-byte parameter limit");
+
 // _nb: kernels without ghost-state code (meshes without boundary sides); _b: with it
 int launch_stage_f32_nb(int order, int equation, const StageArgs &a, cudaStream_t st);
 int launch_stage_f32_b(int order, int equation, const StageArgs &a, cudaStream_t st);
@@ -267,6 +287,18 @@ int launch_batch_stage_f32_nb(int order, int equation, const BatchStageArgs &b, 
 int launch_batch_stage_f32_b(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
 int launch_batch_stage_f64_nb(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
 int launch_batch_stage_f64_b(int order, int equation, const BatchStageArgs &b, cudaStream_t st);
+int launch_batch_param_f32_nb(int order, int equation, const BatchParamArgs &p, int grid, cudaStream_t st);
+int launch_batch_param_f32_b(int order, int equation, const BatchParamArgs &p, int grid, cudaStream_t st);
+int launch_batch_param_f64_nb(int order, int equation, const BatchParamArgs &p, int grid, cudaStream_t st);
+int launch_batch_param_f64_b(int order, int equation, const BatchParamArgs &p, int grid, cudaStream_t st);
+inline int launch_batch_param(int precision, int order, int equation, const BatchParamArgs &p, int grid,
+                              cudaStream_t st) {
+    if (precision == DGX_FP64)
+        return p.bnd ? launch_batch_param_f64_b(order, equation, p, grid, st)
+                     : launch_batch_param_f64_nb(order, equation, p, grid, st);
+    return p.bnd ? launch_batch_param_f32_b(order, equation, p, grid, st)
+                 : launch_batch_param_f32_nb(order, equation, p, grid, st);
+}
 size_t batch_smem_f32(int order, int equation, int nslot, int prefetch_plane);
 size_t batch_smem_f64(int order, int equation, int nslot, int prefetch_plane);
 // the BF16x3 tensor-core kernels (dgx_stage_tc.cu) and their tables

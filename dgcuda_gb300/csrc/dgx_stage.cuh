@@ -1452,6 +1452,70 @@ static int launch_batch_order(int order, const BatchStageArgs &b, cudaStream_t s
     }
 }
 
+// Batched path with the solves' arguments as a kernel parameter: CTA b finds
+// its solve by a binary search of the parameter's tile offsets (uniform over
+// the CTA, served by the constant cache) and runs its tile with the solve's
+// arguments read in place from the parameter space.
+template <int P, int EQ, bool BND>
+__global__ void __launch_bounds__(kTile, min_ctas<P>())
+    batch_stage_kernel_param(const __grid_constant__ BatchParamArgs p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b = static_cast<int>(blockIdx.x);
+    int lo = 0, hi = p.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (p.tile_start[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const int t0 = p.tile_start[lo];
+    const StageArgs &a = p.args[lo];
+    const int tile = b - t0;
+    // a work item outside its solve's tiles (a malformed launch) is skipped
+    // and reported instead of read out of bounds; uniform over the CTA
+    if (tile < 0 || tile * kTile >= a.E) {
+        if (threadIdx.x == 0) atomicOr(a.status, kStatusBadItem);
+        return;
+    }
+    if (threadIdx.x == 0) mbar_init(reinterpret_cast<unsigned long long *>(smem_raw), 1);
+    __syncthreads();
+    stage_tile<P, EQ, BND>(a, tile, smem_raw, 0u);
+}
+
+template <int P, int EQ, bool BND>
+static int launch_batch_param_one(const BatchParamArgs &p, int grid, cudaStream_t st) {
+    constexpr int NV = (EQ == DGX_EULER) ? 4 : 1;
+    const size_t smem = stage_smem_bytes<P, NV>(p.nslot, p.prefetch);
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel_param<P, EQ, BND>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+        DGX_TRY_CUDA(cudaFuncSetAttribute(batch_stage_kernel_param<P, EQ, BND>,
+                                          cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        configured = smem;
+    }
+    if (grid > 0) batch_stage_kernel_param<P, EQ, BND><<<grid, kTile, smem, st>>>(p);
+    DGX_CHECK_LAUNCH();
+    return DGX_OK;
+}
+
+template <int EQ>
+static int launch_batch_param_order(int order, const BatchParamArgs &p, int grid, cudaStream_t st) {
+    switch (order) {
+    case 0: return launch_batch_param_one<0, EQ, kStageBnd>(p, grid, st);
+    case 1: return launch_batch_param_one<1, EQ, kStageBnd>(p, grid, st);
+    case 2: return launch_batch_param_one<2, EQ, kStageBnd>(p, grid, st);
+    case 3: return launch_batch_param_one<3, EQ, kStageBnd>(p, grid, st);
+    case 4: return launch_batch_param_one<4, EQ, kStageBnd>(p, grid, st);
+    case 5: return launch_batch_param_one<5, EQ, kStageBnd>(p, grid, st);
+    default: set_error("unsupported order %d", order); return DGX_ERR_UNSUPPORTED;
+    }
+}
+
+static int launch_batch_param_impl(int order, int equation, const BatchParamArgs &p, int grid, cudaStream_t st) {
+    return equation == DGX_EULER ? launch_batch_param_order<DGX_EULER>(order, p, grid, st)
+                                 : launch_batch_param_order<DGX_ADVECTION>(order, p, grid, st);
+}
+
 template <int EQ>
 static int launch_order(int order, const StageArgs &a, cudaStream_t st) {
     switch (order) {

@@ -17,4 +17,7 @@ size_t batch_smem_f64(int order, int equation, int nslot, int prefetch_plane) {
     return equation == DGX_EULER ? batch_smem_impl<DGX_EULER>(order, nslot, prefetch_plane)
                                  : batch_smem_impl<DGX_ADVECTION>(order, nslot, prefetch_plane);
 }
+int launch_batch_param_f64_nb(int order, int equation, const BatchParamArgs &p, int grid, cudaStream_t st) {
+    return launch_batch_param_impl(order, equation, p, grid, st);
+}
 }  // namespace dgx

@@ -13,4 +13,7 @@ int launch_batch_stage_f64_b(int order, int equation, const BatchStageArgs &b, c
     return equation == DGX_EULER ? launch_batch_order<DGX_EULER>(order, b, st)
                                  : launch_batch_order<DGX_ADVECTION>(order, b, st);
 }
+int launch_batch_param_f64_b(int order, int equation, const BatchParamArgs &p, int grid, cudaStream_t st) {
+    return launch_batch_param_impl(order, equation, p, grid, st);
+}
 }  // namespace dgx
