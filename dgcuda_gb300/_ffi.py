@@ -120,6 +120,8 @@ SIGNATURES = {
     "dgx_batch_launch_count": (None, [_vp, C.POINTER(C.c_longlong)]),
     "dgx_batch_progress": (None, [_vp, _dp, _dp, C.POINTER(C.c_uint), C.POINTER(C.c_longlong), _vp]),
     "dgx_batch_set_options": (None, [_vp, _i, _i, _i]),
+    "dgx_batch_set_fused": (None, [_vp, _i]),
+    "dgx_batch_get_fused": (None, [_vp, _vp, _vp]),
     "dgx_server_create": (None, [_sz, _i, C.POINTER(_vp)]),
     "dgx_server_submit": (None, [_vp, C.POINTER(Request), C.POINTER(C.c_longlong)]),
     "dgx_server_status": (None, [_vp, C.c_longlong, _ip, _dp]),

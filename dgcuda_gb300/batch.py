@@ -39,6 +39,17 @@ class Batch:
                             persistent=v[3].value))
         return out
 
+    def set_fused(self, mode: int) -> None:
+        """0: one launch per class and stage; 2 or 3: one fused launch per stage
+        for every class (the kernel compiled for 2 or 3 CTAs per SM)."""
+        call("dgx_batch_set_fused", self.h, int(mode))
+
+    def fused(self) -> tuple[int, bool]:
+        """(current fused mode, whether the batch allows the fused launch)"""
+        m, a = C.c_int(), C.c_int()
+        call("dgx_batch_get_fused", self.h, C.byref(m), C.byref(a))
+        return m.value, bool(a.value)
+
     def launch_count(self) -> int:
         v = C.c_longlong()
         call("dgx_batch_launch_count", self.h, C.byref(v))

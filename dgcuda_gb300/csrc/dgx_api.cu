@@ -64,6 +64,7 @@ int ensure_device_tables() {
     if (!rc) rc = upload_tables_f64_nb();
     if (!rc) rc = upload_tables_f64_b();
     if (!rc) rc = upload_tables_misc();
+    if (!rc) rc = upload_tables_fused();
     if (!rc) g_tables_ready[dev] = true;
     return rc;
 }

@@ -76,6 +76,15 @@ struct dgx_batch {
     long long dofs = 0;
     long long launches = 0;
     long long launches_per_step = 0;
+    // one launch per stage for every class (dgx_batch_fused.cu): FP32 batches
+    // whose meshes have no boundary sides; 0 off, else the kernel variant (2
+    // or 3 CTAs per SM)
+    int fused = 0;
+    bool fusable = false;
+    StageArgs *d_fargs = nullptr;          // [stage][solve], solves in the items' class order
+    int4 *d_fitems = nullptr;
+    int n_fitems = 0;
+    size_t fsmem = 0;
 };
 
 namespace dgx {
@@ -165,6 +174,8 @@ int class_configure(BatchClass &k) {
     return launch_batch_param(k.precision, k.order, k.equation, pp, 0, nullptr);
 }
 
+int fused_upload(dgx_batch *b);
+
 // Upload the per-solve stage arguments of one class for its current options
 // (the four stages' arrays are contiguous: one copy).
 int class_upload(dgx_batch *b, BatchClass &k) {
@@ -173,7 +184,62 @@ int class_upload(dgx_batch *b, BatchClass &k) {
     if (rc) return rc;
     DGX_TRY_CUDA(cudaMemcpy(k.d_args[0], host.data(), host.size() * sizeof(StageArgs), cudaMemcpyHostToDevice));
     k.h_args = host;
-    return class_configure(k);
+    rc = class_configure(k);
+    if (!rc) rc = fused_upload(b);
+    return rc;
+}
+
+// Order of the classes in the fused work list: costliest tiles first, so the
+// last wave of the launch is filled with the cheapest ones (work per element
+// and stage ~ modes x variables x the volume and side points)
+long long fused_cost(const BatchClass &k) {
+    const int np = (k.order + 1) * (k.order + 2) / 2, nv = k.equation == DGX_EULER ? 4 : 1;
+    return static_cast<long long>(np) * nv * (num_quad(k.order) + 3 * num_quad1(k.order));
+}
+std::vector<int> fused_class_order(const dgx_batch *b) {
+    std::vector<int> ord(b->classes.size());
+    for (size_t c = 0; c < ord.size(); ++c) ord[c] = static_cast<int>(c);
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int x, int y) { return fused_cost(b->classes[x]) > fused_cost(b->classes[y]); });
+    return ord;
+}
+
+// The fused launches' stage arguments: every class's current per-solve
+// arguments (its own options), in the work list's class order; and the
+// launch's shared memory, the largest any class needs.
+int fused_upload(dgx_batch *b) {
+    if (!b->fusable) return DGX_OK;
+    const std::vector<int> ord = fused_class_order(b);
+    size_t ns = 0;
+    for (auto &k : b->classes) ns += k.solves.size();
+    std::vector<StageArgs> host(4 * ns);
+    size_t base = 0, smem = 0;
+    for (int c : ord) {
+        const BatchClass &k = b->classes[c];
+        const size_t n = k.solves.size();
+        for (int stage = 0; stage < 4; ++stage)
+            for (size_t j = 0; j < n; ++j) host[stage * ns + base + j] = k.h_args[stage * n + j];
+        base += n;
+        smem = std::max(smem, batch_smem_f32(k.order, k.equation, k.nslot, k.prefetch ? k.pre_plane : 0));
+    }
+    DGX_TRY_CUDA(cudaMemcpy(b->d_fargs, host.data(), host.size() * sizeof(StageArgs), cudaMemcpyHostToDevice));
+    b->fsmem = smem;
+    // set the kernels' shared-memory limits outside any capture (no launch)
+    for (int v = 2; v <= 3; ++v) {
+        FusedStageArgs f{b->d_fargs, b->d_fitems, 0, v};
+        const int rc = launch_batch_fused_f32(f, smem, nullptr);
+        if (rc) return rc;
+    }
+    return DGX_OK;
+}
+
+int fused_launch(dgx_batch *b, int stage, cudaStream_t st) {
+    size_t ns = 0;
+    for (auto &k : b->classes) ns += k.solves.size();
+    FusedStageArgs f{b->d_fargs + stage * ns, b->d_fitems, b->n_fitems, b->fused};
+    const int rc = launch_batch_fused_f32(f, b->fsmem, st);
+    if (!rc && b->n_fitems > 0) b->launches++;
+    return rc;
 }
 
 // one step without the graph
@@ -181,6 +247,10 @@ int step_direct(dgx_batch *b, cudaStream_t st) {
     int rc = launch_batch_dt(b->d_dt, b->d_cfl_items, b->n_cfl_items, st);
     if (rc) return rc;
     b->launches++;
+    if (b->fused) {
+        for (int stage = 0; stage < 4 && !rc; ++stage) rc = fused_launch(b, stage, st);
+        return rc;
+    }
     for (auto &k : b->classes)
         for (int stage = 0; stage < 4; ++stage) {
             rc = class_launch(b, k, stage, st);
@@ -205,8 +275,10 @@ int build_graph(dgx_batch *b) {
     int rc = launch_batch_dt(b->d_dt, b->d_cfl_items, b->n_cfl_items, b->cap);
     b->launches++;
     if (!rc) rc = cudaEventRecord(b->start, b->cap) == cudaSuccess ? DGX_OK : DGX_ERR_CUDA;
+    // fused: the four stage launches of every class on the capture stream
+    for (int stage = 0; b->fused && stage < 4 && !rc; ++stage) rc = fused_launch(b, stage, b->cap);
     for (auto &k : b->classes) {
-        if (rc) break;
+        if (rc || b->fused) break;
         if (cudaStreamWaitEvent(k.stream, b->start, 0) != cudaSuccess) { rc = DGX_ERR_CUDA; break; }
         for (int stage = 0; stage < 4 && !rc; ++stage) rc = class_launch(b, k, stage, k.stream);
         if (!rc && cudaEventRecord(k.done, k.stream) != cudaSuccess) rc = DGX_ERR_CUDA;
@@ -327,6 +399,23 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
         if (!rc) k.h_args = args[c];
     }
     if (rc) { batch_free(b); return rc; }
+    // the fused work list: (index into the fused arguments, tile, class code),
+    // costliest classes first
+    b->fusable = true;
+    for (auto &k : b->classes)
+        if (k.precision != DGX_FP32 || k.bnd || k.order > kFusedMaxOrder) b->fusable = false;
+    std::vector<int4> fitems;
+    if (b->fusable) {
+        int base = 0;
+        for (int c : fused_class_order(b)) {
+            const BatchClass &k = b->classes[c];
+            const int code = 2 * k.order + (k.equation == DGX_EULER ? 1 : 0);
+            for (size_t j = 0; j < k.solves.size(); ++j)
+                for (int t = 0; t < k.tiles[j]; ++t) fitems.push_back(make_int4(base + static_cast<int>(j), t, code, 0));
+            base += static_cast<int>(k.solves.size());
+        }
+        b->n_fitems = static_cast<int>(fitems.size());
+    }
     // one device block for every array of the batch, filled by one copy
     BlockLayout L;
     const size_t oScal = L.take<const double *>(n), oStat = L.take<const unsigned int *>(n),
@@ -336,8 +425,10 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
         oArgs[c] = L.take<StageArgs>(args[c].size());
         oItems[c] = L.take<int2>(items[c].size());
     }
+    const size_t oFItems = L.take<int4>(fitems.size());
     const size_t upload = L.size;
     const size_t oProg = L.take<double>(4 * static_cast<size_t>(n));
+    const size_t oFArgs = L.take<StageArgs>(b->fusable ? 4 * static_cast<size_t>(n) : 0);
     rc = block_alloc(b->block, L.size, nullptr);
     if (rc) { batch_free(b); return rc; }
     std::vector<unsigned char> stage(upload, 0);
@@ -358,6 +449,7 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
         put(oSteps, stp.data(), sizeof(long long *) * n);
     }
     put(oDt, dts.data(), sizeof(DtArgs) * n);
+    put(oFItems, fitems.data(), sizeof(int4) * fitems.size());
     put(oCfl, cfl_items.data(), sizeof(int2) * cfl_items.size());
     for (size_t c = 0; c < b->classes.size(); ++c) {
         put(oArgs[c], args[c].data(), sizeof(StageArgs) * args[c].size());
@@ -369,6 +461,8 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
     b->d_dt = block_at<DtArgs>(b->block, oDt);
     b->d_cfl_items = block_at<int2>(b->block, oCfl);
     b->d_progress = block_at<double>(b->block, oProg);
+    b->d_fitems = block_at<int4>(b->block, oFItems);
+    b->d_fargs = block_at<StageArgs>(b->block, oFArgs);
     b->h_progress.assign(4 * static_cast<size_t>(n), 0.0);
     for (size_t c = 0; c < b->classes.size(); ++c) {
         BatchClass &k = b->classes[c];
@@ -388,6 +482,7 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
         if (!rc) rc = class_configure(k);
         if (rc) break;
     }
+    if (!rc) rc = fused_upload(b);
     if (!rc && (cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess ||
                 cudaEventCreateWithFlags(&b->start, cudaEventDisableTiming) != cudaSuccess))
         rc = DGX_ERR_CUDA;
@@ -475,6 +570,24 @@ int dgx_batch_set_options(dgx_batch *b, int cls, int prefetch, int persistent) {
     return rc;
 }
 
+int dgx_batch_set_fused(dgx_batch *b, int mode) {
+    if (!b || (mode != 0 && mode != 2 && mode != 3)) { set_error("fused mode is 0, 2 or 3"); return DGX_ERR_INVALID; }
+    if (mode && !b->fusable) {
+        set_error("the fused launch takes FP32 batches whose meshes have no boundary sides, orders up to %d",
+                  kFusedMaxOrder);
+        return DGX_ERR_UNSUPPORTED;
+    }
+    b->fused = mode;
+    return build_graph(b);
+}
+
+int dgx_batch_get_fused(const dgx_batch *b, int *mode, int *available) {
+    if (!b) return DGX_ERR_INVALID;
+    if (mode) *mode = b->fused;
+    if (available) *available = b->fusable ? 1 : 0;
+    return DGX_OK;
+}
+
 int dgx_batch_launch_count(const dgx_batch *b, long long *count) {
     if (!b || !count) return DGX_ERR_INVALID;
     *count = b->launches;
@@ -534,6 +647,27 @@ int dgx_batch_autotune(dgx_batch *b, int reps, void *stream) {
         k.prefetch = bp;
         k.persistent = bq;
         if (!rc) rc = class_upload(b, k);
+    }
+    // then the whole step: the tuned per-class launches against the fused
+    // launch of both variants (graph steps; the states are restored below)
+    if (!rc && b->fusable) {
+        float best = 1e30f;
+        int bf = 0;
+        for (int mode : {0, 2, 3}) {
+            b->fused = mode;
+            rc = build_graph(b);
+            if (rc) break;
+            if (cudaGraphLaunch(b->exec, st) != cudaSuccess) { rc = DGX_ERR_CUDA; break; }
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < reps && !rc; ++r)
+                if (cudaGraphLaunch(b->exec, st) != cudaSuccess) rc = DGX_ERR_CUDA;
+            cudaEventRecord(e1, st);
+            if (rc || cudaEventSynchronize(e1) != cudaSuccess) { rc = rc ? rc : DGX_ERR_CUDA; break; }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) { best = ms; bf = mode; }
+        }
+        b->fused = bf;
     }
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);

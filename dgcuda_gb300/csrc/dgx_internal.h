@@ -301,6 +301,20 @@ inline int launch_batch_param(int precision, int order, int equation, const Batc
 }
 size_t batch_smem_f32(int order, int equation, int nslot, int prefetch_plane);
 size_t batch_smem_f64(int order, int equation, int nslot, int prefetch_plane);
+
+// One launch per RK stage for every FP32 solve of a batch whose meshes have no
+// boundary sides, whatever its order and equation (dgx_batch_fused.cu): CTA b
+// runs item b, items[b] = (index into args, tile, class code 2*order +
+// equation, 0); the items of the costliest classes come first.
+struct FusedStageArgs {
+    const StageArgs *args;   // this stage's arguments of every solve in the launch
+    const int4 *items;
+    int n_items;
+    int min_ctas;            // 2 or 3: the kernel variant (CTAs per SM it is compiled for)
+};
+constexpr int kFusedMaxOrder = 5;
+int launch_batch_fused_f32(const FusedStageArgs &f, size_t smem, cudaStream_t st);
+int upload_tables_fused();
 // the BF16x3 tensor-core kernels (dgx_stage_tc.cu) and their tables
 int launch_stage_tc(int order, int equation, const StageArgs &a, cudaStream_t st);
 int upload_tables_tc();

@@ -341,9 +341,22 @@ int dgx_batch_step(dgx_batch *batch, void *stream);
 int dgx_batch_run(dgx_batch *batch, int steps, void *stream);
 /* Choose per class, by timing `reps` stage launches on the live batch, the
  * kernel options (TMA prefetch of the epilogue operands; flat grid or a
- * persistent grid of 2 or 4 CTAs per SM), then rebuild the graph.  The solves'
- * states and times are restored afterwards.  Synchronous. */
+ * persistent grid of 2 or 4 CTAs per SM); then, where the batch allows the
+ * fused launch (below), choose between the per-class launches and the fused
+ * launch's two variants by timing `reps` whole steps; rebuild the graph.  The
+ * solves' states and times are restored afterwards.  Synchronous. */
 int dgx_batch_autotune(dgx_batch *batch, int reps, void *stream);
+/* The fused launch: one kernel per RK stage for every class of the batch (a
+ * step is the dt launch and four stage launches) over one work list of
+ * (solve, tile) items, the costliest classes first.  FP32 batches whose meshes
+ * have no boundary sides (others: DGX_ERR_UNSUPPORTED).  mode 0: the
+ * per-class launches (default); 2 or 3: the fused kernel compiled for 2 or 3
+ * CTAs per SM (one register count for every class: 2 keeps order-4 Euler
+ * unspilled, 3 caps every class at 168 registers).  Results are the same bits
+ * either way.  Rebuilds the graph.  No counterpart in the reference. */
+int dgx_batch_set_fused(dgx_batch *batch, int mode);
+/* the current mode, and whether the batch allows the fused launch */
+int dgx_batch_get_fused(const dgx_batch *batch, int *mode, int *available);
 int dgx_batch_info(const dgx_batch *batch, int *num_classes, int *num_items, long long *dofs,
                    long long *launches_per_step);
 int dgx_batch_class_options(const dgx_batch *batch, int cls, int *order, int *equation,

@@ -85,3 +85,63 @@ def test_batch_rejects_duplicates(gpu):
     sv = make(CASES[0], 0)
     with pytest.raises(_ffi.DgxError):
         Batch([sv, sv])
+
+
+FP32_CASES = [c for c in CASES if c[3] == _ffi.FP32]
+
+
+@pytest.mark.parametrize("mode", [2, 3])
+def test_fused_launch_equals_solves_alone(mode, gpu):
+    """One kernel per RK stage for every class (a step is 5 launches); each
+    solve still equals the same solve run alone, bit for bit."""
+    alone = [make(c, i) for i, c in enumerate(FP32_CASES)]
+    mixed = [make(c, i) for i, c in enumerate(FP32_CASES)]
+    for sv in alone:
+        sv.run(max_steps=6)
+    b = Batch(mixed)
+    assert b.fused() == (0, True)
+    b.set_fused(mode)
+    assert b.fused() == (mode, True)
+    info = b.info()
+    assert info["launches_per_step"] == 5
+    b.run(6)
+    torch.cuda.synchronize()
+    for a, m in zip(alone, mixed):
+        np.testing.assert_array_equal(m.get_state(), a.get_state())
+        assert a.time() == m.time()
+    assert b.launch_count() == 6 * 5
+    # back to the per-class launches mid-run: the same bits again
+    b.set_fused(0)
+    assert b.info()["launches_per_step"] == 1 + 4 * len({(c[0], c[1]) for c in FP32_CASES})
+    for sv in alone:
+        sv.run(max_steps=2)
+    b.run(2)
+    torch.cuda.synchronize()
+    for a, m in zip(alone, mixed):
+        np.testing.assert_array_equal(m.get_state(), a.get_state())
+
+
+def test_fused_launch_refused_where_unsupported(gpu):
+    """FP64 solves (and meshes with boundary sides) keep the per-class launches."""
+    b = Batch([make(c, i) for i, c in enumerate(CASES)])   # includes an FP64 solve
+    assert b.fused() == (0, False)
+    with pytest.raises(_ffi.DgxError):
+        b.set_fused(2)
+    with pytest.raises(_ffi.DgxError):
+        Batch([make(FP32_CASES[0], 0)]).set_fused(1)        # not a variant
+
+
+def test_autotune_may_choose_fused(gpu):
+    alone = [make(c, i) for i, c in enumerate(FP32_CASES)]
+    mixed = [make(c, i) for i, c in enumerate(FP32_CASES)]
+    for sv in alone:
+        sv.run(max_steps=5)
+    b = Batch(mixed)
+    b.run(2)
+    b.autotune(reps=2)
+    mode, avail = b.fused()
+    assert avail and mode in (0, 2, 3)
+    b.run(3)
+    torch.cuda.synchronize()
+    for a, m in zip(alone, mixed):
+        np.testing.assert_array_equal(m.get_state(), a.get_state())
