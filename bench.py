@@ -285,11 +285,12 @@ def _config4_requests(seed: int, count: int, n_lo: int, n_hi: int):
     return out
 
 
-def _native_solver(spec):
+def _native_solver(spec, precision=None):
     from dgcuda_gb300 import _ffi
     from dgcuda_gb300.solver import DeviceMesh, Solver
     dm = DeviceMesh.periodic_square(spec["n"], spec["lx"], spec["ly"], spec["jitter"], spec["seed"])
-    sv = Solver(dm, spec["order"], spec["equation"], _ffi.FLUX_LLF, _ffi.FP32, 1.4)
+    sv = Solver(dm, spec["order"], spec["equation"], _ffi.FLUX_LLF,
+                _ffi.FP32 if precision is None else precision, 1.4)
     sv.project(spec["ic"], spec["params"])
     sv.set_dt(None, cfl=0.7)
     return sv
@@ -394,6 +395,7 @@ def run_batched(steps: int = 20):
     accuracy = _sample_accuracy(specs, solvers, sampled[0], states=sampled[1])
     for sv in solvers:
         sv.close()
+    compensated = _batched_compensated(specs, steps)
     return {"workload": "256 solves: equation 50/50, N log-uniform [16,512] (2N^2 triangles), "
                         "p uniform 1..4, Gaussian pulses / isentropic vortices, FP32, CFL 0.7",
             "dofs_per_step": dofs, "elements": int(sum(2 * sp["n"] ** 2 for sp in specs)),
@@ -402,7 +404,53 @@ def run_batched(steps: int = 20):
             "speedup_vs_plain": plain_ms / batch_ms, "classes": info["classes"],
             "work_items": info["items"], "launches_per_step": launches_per_step,
             "launch_mode": {0: "per_class", 2: "fused_2cta", 3: "fused_3cta"}[chosen],
-            "launch_modes": modes, "tuned_options": opts, "accuracy": accuracy, "unit": UNIT}
+            "launch_modes": modes, "tuned_options": opts, "accuracy": accuracy, "compensated": compensated,
+            "unit": UNIT}
+
+
+def _batched_compensated(specs, steps):
+    """The batched configuration in the compensated FP32 precision
+    (DGX_FP32_COMP): the same solves one by one and batched (per-class
+    launches, default options), 2 x (3 + steps) steps in all, then the same
+    accuracy sample against the FP64 path as the FP32 run."""
+    import torch
+    from dgcuda_gb300 import _ffi
+    from dgcuda_gb300.batch import Batch
+    solvers = [_native_solver(sp, _ffi.FP32_COMP) for sp in specs]
+    dofs = sum(sv.nv * sv.np * sv.E for sv in solvers)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            for sv in solvers:
+                sv.step(sh)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(steps):
+            for sv in solvers:
+                sv.step(sh)
+        b.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = a.elapsed_time(b) / steps
+        bt = Batch(solvers)
+        for _ in range(3):
+            bt.step(sh)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(steps):
+            bt.step(sh)
+        b.record(stream)
+        torch.cuda.synchronize()
+        batch_ms = a.elapsed_time(b) / steps
+    bt.close()
+    accuracy = _sample_accuracy(specs, solvers, 2 * (3 + steps))
+    for sv in solvers:
+        sv.close()
+    return {"precision": "fp32_comp (compensated accumulation of the RK4 increments)",
+            "value": dofs / (batch_ms * 1e-3), "ms_per_step": batch_ms,
+            "plain_value": dofs / (plain_ms * 1e-3), "plain_ms_per_step": plain_ms,
+            "speedup_vs_plain": plain_ms / batch_ms, "accuracy": accuracy, "unit": UNIT}
 
 
 def _sample_accuracy(specs, solvers, nsteps, every: int = 16, states=None):
@@ -617,24 +665,50 @@ def run_served_stated(rates=(50, 200, 1000, 2000), arrive_s=6.0, serve_s=12.0, c
                    "completed": srv_rec["completed"], "p50_s": srv_rec["p50_s"], "p99_s": srv_rec["p99_s"]},
         "plain": {"wall_s": pwall, "value": pdof / pwall},
         "served_vs_plain": (srv_rec["dof_updates"] / srv_rec["wall_s"]) / (pdof / pwall) if pdof else None}
-    rows, worst = [], [0.0] * 4
-    for k, (c, steps, t) in kept.items():
+    # the same requests in the compensated FP32 precision, both paths
+    csub = [dict(sp, precision=_ffi.FP32_COMP) for sp in sub]
+    csrv_rec, ckept = _serve_window(csub, 0, 0.0, 600.0, keep=range(8))
+    t0, cdof = time.perf_counter(), 0.0
+    for sp in sub:
+        sv = _native_solver(sp, _ffi.FP32_COMP)
+        n, _ = sv.run(t_end=sp["t_end"])
+        cdof += n * sv.nv * sv.np * sv.E
+        sv.close()
+    torch.cuda.synchronize()
+    cwall = time.perf_counter() - t0
+    out["same_requests_compensated"] = {
+        "precision": "fp32_comp (compensated accumulation of the RK4 increments)",
+        "served": {"wall_s": csrv_rec["wall_s"], "value": csrv_rec["dof_updates"] / csrv_rec["wall_s"],
+                   "completed": csrv_rec["completed"], "p50_s": csrv_rec["p50_s"], "p99_s": csrv_rec["p99_s"]},
+        "plain": {"wall_s": cwall, "value": cdof / cwall},
+        "served_vs_plain": (csrv_rec["dof_updates"] / csrv_rec["wall_s"]) / (cdof / cwall) if cdof else None}
+
+    def accuracy_of(kept_states):
+        rows, worst = [], [0.0] * 4
+        for k, (c, steps, t) in kept_states.items():
+            sp = sub[k]
+            b = refs[k]
+            err = [float(np.linalg.norm(c[n] - b[n]) / np.linalg.norm(b[n])) for n in range(c.shape[0])]
+            for n, v in enumerate(err):
+                worst[n] = max(worst[n], v)
+            rows.append({"request": sel[k], "n": sp["n"], "order": sp["order"], "steps": steps,
+                         "equation": "euler" if sp["equation"] == _ffi.EULER else "advection", "rel_l2": err})
+        return {"reference": "the same request in FP64 on the GPU, to the same end time",
+                "max_rel_l2_per_variable": worst, "max_rel_l2": max(worst) if rows else None,
+                "meets_1e-5": (max(worst) <= 1e-5) if rows else None, "sample": rows}
+
+    refs = {}
+    for k in set(kept) | set(ckept):
         sp = sub[k]
         dm = DeviceMesh.periodic_square(sp["n"], sp["lx"], sp["ly"], sp["jitter"], sp["seed"])
         ref = Solver(dm, sp["order"], sp["equation"], _ffi.FLUX_LLF, _ffi.FP64, 1.4)
         ref.project(sp["ic"], sp["params"])
         ref.set_dt(None, cfl=0.7)
         ref.run(t_end=sp["t_end"])
-        b = ref.get_state()
+        refs[k] = ref.get_state()
         ref.close()
-        err = [float(np.linalg.norm(c[n] - b[n]) / np.linalg.norm(b[n])) for n in range(c.shape[0])]
-        for n, v in enumerate(err):
-            worst[n] = max(worst[n], v)
-        rows.append({"request": sel[k], "n": sp["n"], "order": sp["order"], "steps": steps,
-                     "equation": "euler" if sp["equation"] == _ffi.EULER else "advection", "rel_l2": err})
-    out["accuracy"] = {"reference": "the same request in FP64 on the GPU, to the same end time",
-                       "max_rel_l2_per_variable": worst, "max_rel_l2": max(worst) if rows else None,
-                       "meets_1e-5": (max(worst) <= 1e-5) if rows else None, "sample": rows}
+    out["accuracy"] = accuracy_of(kept)
+    out["accuracy_compensated"] = accuracy_of(ckept)
     return out
 
 
@@ -716,6 +790,22 @@ def run_fp64(mesh, args, dofs, steps: int = 10):
             "gpu_launches": launches,
             "what": "the FP64 path (scalar FP64 stage kernel, FP64 state) on the same workload; compare with "
                     "the reference arm's reference_gpu (the reference's CUDA solver, FP64)"}
+
+
+def run_fp32_comp(mesh, args, dofs, fp32_ms, steps: int = 50):
+    """The same workload in the compensated FP32 precision (DGX_FP32_COMP:
+    the RK4 increments accumulated apart from the state, the state carried as
+    c + lo): step time beside the plain FP32 path's."""
+    import torch
+    from dgcuda_gb300 import _ffi
+    sv = density_wave_solver(mesh, _ffi.FP32_COMP)
+    stream = torch.cuda.Stream()
+    ms, stage_ms, launches, _, _ = time_steps(sv, steps, 3, stream, 1)
+    sv.close()
+    return {"value": dofs / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": steps, "dtype": "f32",
+            "gpu_launches": launches, "time_vs_fp32": ms / fp32_ms,
+            "what": "FP32 state and arithmetic, RK4 increments accumulated apart from the state and the "
+                    "state updated by an error-free two-sum (19 state passes per step instead of 13)"}
 
 
 def run_ours(args, rank, world, local):
@@ -814,6 +904,7 @@ def run_ours(args, rank, world, local):
     if not args.no_extra and prec == _ffi.FP32:
         out["bf16x3"] = run_bf16x3(mesh, args, stage_bytes, peak, dofs, ms_step)
         out["fp64"] = run_fp64(mesh, args, dofs)
+        out["fp32_comp"] = run_fp32_comp(mesh, args, dofs, ms_step)
         out["accuracy"] = run_accuracy(args.mesh_n)
         out["batched"] = run_batched()
         out["served"] = run_served_stated()

@@ -18,7 +18,7 @@ ERR_NONFINITE, ERR_BUSY, ERR_NOT_FOUND, ERR_TIMEOUT = -5, -6, -7, -8
 
 ADVECTION, EULER = 0, 1
 FLUX_CENTRAL, FLUX_LLF = 0, 1
-FP32, FP32_BF16X3, FP64 = 0, 1, 2
+FP32, FP32_BF16X3, FP64, FP32_COMP = 0, 1, 2, 3
 RK4, RK2, FE = 0, 1, 2
 DT_FIXED, DT_CFL = 0, 1
 OPT_PREFETCH, OPT_STAGE_TIME, OPT_LIMITER, OPT_HOOK_MATH = 1, 2, 3, 4

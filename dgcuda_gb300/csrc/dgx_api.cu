@@ -209,7 +209,8 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
     a.ayf = static_cast<float>(s.ay);
     // the epilogue operands of stages 2-4 are the solver's own buffers (16-byte
     // slack at their end for the widened prefetch slices)
-    if (s.prefetch && mode >= 2 && mode <= 4 && c && acc) {
+    const bool comp_pre = s.precision == DGX_FP32_COMP && mode == 1;   // the low part into stage 1
+    if (s.prefetch && ((mode >= 2 && mode <= 4) || comp_pre) && c && acc) {
         const int align = 16 / static_cast<int>(elem_size(s));   // values per 16 bytes
         a.prefetch = m.num_elem % align == 0 ? kTile : kTile + align;
     } else {
@@ -252,6 +253,7 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
     }
     a.aux = nullptr;
     a.rk13 = 0;
+    a.comp = 0;
     return a;
 }
 
@@ -266,9 +268,18 @@ StageArgs make_stage_args(dgx_solver *sv, int mode, const void *u, const void *c
 // The differences u2 - c, u3 - c are exact (Sterbenz) for steps that change a
 // coefficient by less than half its value, so the accumulator's rounding is
 // of the order of the 16-pass form's.
+//
+// DGX_FP32_COMP keeps the increments apart from the state and the state as
+// c + lo (19 state passes: 4, 5, 5, 5): stage 1 reads c and lo and writes
+// u2 = c + k1/2 and D = lo + k1/6 (in acc); stages 2, 3 read their input, c and
+// D and write u3 = c + k2/2 (u4 = c + k3) and D + k/3; stage 4 reads u4, c and
+// D and writes the two-sum of c and D + k4/6 as the new (c, lo).  The FP32
+// rounding of u2..u4, which only feed the right-hand sides, costs ~1e-7 over
+// thousands of steps; the rounding of a stored state, which the plain forms
+// accumulate step after step, none.
 StageArgs rk4_stage_args(dgx_solver *sv, int stage) {
     SolverDev &s = sv->s;
-    const bool rk13 = !s.limiter;
+    const bool rk13 = !s.limiter && s.precision != DGX_FP32_COMP;
     StageArgs a;
     switch (stage) {
     case 0: a = make_stage_args(sv, 1, s.c, s.c, s.acc, s.ua, 0.0, 0.0); break;
@@ -278,6 +289,10 @@ StageArgs rk4_stage_args(dgx_solver *sv, int stage) {
     }
     a.rk13 = rk13 ? 1 : 0;
     if (rk13 && stage == 2) a.aux = s.ua;   // u2, overwritten in place by u4
+    if (s.precision == DGX_FP32_COMP) {
+        a.comp = 1;
+        if (stage == 0 || stage == 3) a.aux = s.lo;   // read by stage 1, written by stage 4
+    }
     return a;
 }
 
@@ -399,9 +414,14 @@ int solver_build(dgx_mesh *mesh, const dgx_solver_desc *desc, BlockPool *pool, c
     if (desc->order < 0 || desc->order > kMaxOrder) { set_error("order %d outside 0..%d", desc->order, kMaxOrder); return DGX_ERR_UNSUPPORTED; }
     if (desc->equation != DGX_ADVECTION && desc->equation != DGX_EULER) { set_error("unknown equation"); return DGX_ERR_INVALID; }
     if (desc->flux != DGX_FLUX_CENTRAL && desc->flux != DGX_FLUX_LLF) { set_error("unknown flux"); return DGX_ERR_INVALID; }
-    if (desc->precision != DGX_FP32 && desc->precision != DGX_FP64 && desc->precision != DGX_FP32_BF16X3) {
+    if (desc->precision != DGX_FP32 && desc->precision != DGX_FP64 && desc->precision != DGX_FP32_BF16X3 &&
+        desc->precision != DGX_FP32_COMP) {
         set_error("unknown precision %d", desc->precision);
         return DGX_ERR_INVALID;
+    }
+    if (desc->precision == DGX_FP32_COMP && desc->integrator != DGX_RK4) {
+        set_error("the compensated FP32 precision serves RK4");
+        return DGX_ERR_UNSUPPORTED;
     }
     if (desc->precision == DGX_FP32_BF16X3) {
         if (desc->order < kTcMinOrder || desc->order > kTcMaxOrder) {
@@ -440,8 +460,8 @@ int solver_build(dgx_mesh *mesh, const dgx_solver_desc *desc, BlockPool *pool, c
     constexpr size_t kHdr = 96;
     BlockLayout L;
     const size_t oHdr = L.take<unsigned char>(kHdr);
-    const int nbuf = s.integrator == DGX_RK4 ? 4 : 2;
-    size_t oBuf[4] = {0, 0, 0, 0};
+    const int nbuf = s.integrator == DGX_RK4 ? (s.precision == DGX_FP32_COMP ? 5 : 4) : 2;
+    size_t oBuf[5] = {0, 0, 0, 0, 0};
     for (int i = 0; i < nbuf; ++i) oBuf[i] = L.take<unsigned char>(s.n * es + 64);
     rc = block_alloc(sv->block, L.size, pool);
     if (rc) { delete sv; return rc; }
@@ -452,14 +472,15 @@ int solver_build(dgx_mesh *mesh, const dgx_solver_desc *desc, BlockPool *pool, c
     s.status = reinterpret_cast<unsigned int *>(hdr + 76);
     s.steps = reinterpret_cast<long long *>(hdr + 80);
     s.chg_bits = reinterpret_cast<unsigned long long *>(hdr + 88);
-    void *bufs[4] = {nullptr, nullptr, nullptr, nullptr};
+    void *bufs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     for (int i = 0; i < nbuf; ++i) bufs[i] = block_at<unsigned char>(sv->block, oBuf[i]);
-    s.c = bufs[0]; s.ua = bufs[1]; s.acc = bufs[2]; s.ub = bufs[3];
+    s.c = bufs[0]; s.ua = bufs[1]; s.acc = bufs[2]; s.ub = bufs[3]; s.lo = bufs[4];
     // the scalars by a kernel (its arguments are captured at launch): a copy
     // from pageable memory would first wait for the stream
     const double def[8] = {0.0, 0.0, 0.0, 0.0, 0.7, 0.0, 0.0, 0.0};
     rc = init_solver_scalars(hdr, scal_init ? scal_init : def, st);
     cudaError_t ce = rc ? cudaErrorLaunchFailure : cudaMemsetAsync(s.c, 0, s.n * es, st);
+    if (ce == cudaSuccess && s.lo) ce = cudaMemsetAsync(s.lo, 0, s.n * es, st);
     if (ce != cudaSuccess) {
         set_error("solver init failed: %s", cudaGetErrorString(ce));
         cudaStreamSynchronize(st);
@@ -604,6 +625,10 @@ int dgx_set_state(dgx_solver *sv, const double *c) {
         std::vector<float> tmp(s.n);
         for (size_t i = 0; i < s.n; ++i) tmp[i] = static_cast<float>(c[i]);
         DGX_TRY_CUDA(cudaMemcpy(s.c, tmp.data(), s.n * sizeof(float), cudaMemcpyHostToDevice));
+        if (s.lo) {   // the part of each value the FP32 state does not hold
+            for (size_t i = 0; i < s.n; ++i) tmp[i] = static_cast<float>(c[i] - static_cast<double>(static_cast<float>(c[i])));
+            DGX_TRY_CUDA(cudaMemcpy(s.lo, tmp.data(), s.n * sizeof(float), cudaMemcpyHostToDevice));
+        }
     }
     return DGX_OK;
 }
@@ -618,6 +643,10 @@ int dgx_get_state(dgx_solver *sv, double *c) {
         std::vector<float> tmp(s.n);
         DGX_TRY_CUDA(cudaMemcpy(tmp.data(), s.c, s.n * sizeof(float), cudaMemcpyDeviceToHost));
         for (size_t i = 0; i < s.n; ++i) c[i] = tmp[i];
+        if (s.lo) {   // state = c + lo
+            DGX_TRY_CUDA(cudaMemcpy(tmp.data(), s.lo, s.n * sizeof(float), cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < s.n; ++i) c[i] += tmp[i];
+        }
     }
     return DGX_OK;
 }
@@ -627,6 +656,7 @@ int dgx_set_state_f32(dgx_solver *sv, const float *c, void *stream) {
     SolverDev &s = sv->s;
     if (s.precision != DGX_FP64) {
         DGX_TRY_CUDA(cudaMemcpyAsync(s.c, c, s.n * sizeof(float), cudaMemcpyHostToDevice, as_stream(stream)));
+        if (s.lo) DGX_TRY_CUDA(cudaMemsetAsync(s.lo, 0, s.n * sizeof(float), as_stream(stream)));
         return DGX_OK;
     }
     // stage through the (between steps unused) stage-input buffer, then widen on the device
@@ -678,6 +708,7 @@ int project_ic_on(dgx_solver *sv, int ic, const double *params, cudaStream_t st)
     int rc = project_ic(sv->s, sv->mesh->d, ic, params, st);
     if (rc) return rc;
     sv->launches++;
+    if (sv->s.lo) DGX_TRY_CUDA(cudaMemsetAsync(sv->s.lo, 0, sv->s.n * sizeof(float), st));   // state = c
     return DGX_OK;
 }
 
@@ -828,6 +859,10 @@ int dgx_solver_set_option(dgx_solver *sv, int option, int value) {
     case DGX_OPT_PREFETCH: sv->s.prefetch = value ? 1 : 0; return DGX_OK;
     case DGX_OPT_LIMITER:
         if (value && sv->s.order != 1) { set_error("the limiter serves p = 1"); return DGX_ERR_UNSUPPORTED; }
+        if (value && sv->s.precision == DGX_FP32_COMP) {
+            set_error("the limiter changes stage states the compensated precision keeps apart from its increments");
+            return DGX_ERR_UNSUPPORTED;
+        }
         sv->s.limiter = value ? 1 : 0;
         return DGX_OK;
     case DGX_OPT_STAGE_TIME:

@@ -97,7 +97,8 @@ int class_launch(dgx_batch *b, BatchClass &k, int stage, cudaStream_t st) {
         const size_t ns = k.solves.size();
         static thread_local BatchParamArgs p;
         p.nslot = k.nslot;
-        p.prefetch = (stage >= 1 && k.prefetch) ? k.pre_plane : 0;
+        // stage 1 of a compensated class prefetches the state's low part
+        p.prefetch = ((stage >= 1 || k.precision == DGX_FP32_COMP) && k.prefetch) ? k.pre_plane : 0;
         p.bnd = k.bnd;
         for (size_t j0 = 0; j0 < ns; j0 += kParamSolves) {
             const int n = static_cast<int>(std::min<size_t>(kParamSolves, ns - j0));
@@ -120,7 +121,7 @@ int class_launch(dgx_batch *b, BatchClass &k, int stage, cudaStream_t st) {
     a.items = k.d_items;
     a.n_items = k.n_items;
     a.nslot = k.nslot;
-    a.prefetch = (stage >= 1 && k.prefetch) ? k.pre_plane : 0;
+    a.prefetch = ((stage >= 1 || k.precision == DGX_FP32_COMP) && k.prefetch) ? k.pre_plane : 0;
     a.bnd = k.bnd;
     if (k.persistent > 0) a.grid = std::min(k.n_items, num_sms() * k.persistent);
     else a.grid = k.n_items;
@@ -403,7 +404,8 @@ int dgx_batch_create(dgx_solver *const *solvers, int n, dgx_batch **out) {
     // costliest classes first
     b->fusable = true;
     for (auto &k : b->classes)
-        if (k.precision != DGX_FP32 || k.bnd || k.order > kFusedMaxOrder) b->fusable = false;
+        if ((k.precision != DGX_FP32 && k.precision != DGX_FP32_COMP) || k.bnd || k.order > kFusedMaxOrder)
+            b->fusable = false;
     std::vector<int4> fitems;
     if (b->fusable) {
         int base = 0;
@@ -604,7 +606,7 @@ int dgx_batch_autotune(dgx_batch *b, int reps, void *stream) {
     DGX_TRY_CUDA(cudaStreamSynchronize(st));
     // save
     const size_t n = b->solvers.size();
-    std::vector<void *> saved(n, nullptr);
+    std::vector<void *> saved(n, nullptr), saved_lo(n, nullptr);
     std::vector<double> scal(8 * n);
     std::vector<long long> steps(n);
     int rc = DGX_OK;
@@ -612,6 +614,12 @@ int dgx_batch_autotune(dgx_batch *b, int reps, void *stream) {
         SolverDev &s = b->solvers[i]->s;
         const size_t bytes = s.n * (s.precision == DGX_FP64 ? 8 : 4);
         if (cudaMalloc(&saved[i], bytes) != cudaSuccess) { set_error("autotune backup allocation failed"); rc = DGX_ERR_NOMEM; break; }
+        if (s.lo && (cudaMalloc(&saved_lo[i], bytes) != cudaSuccess ||
+                     cudaMemcpy(saved_lo[i], s.lo, bytes, cudaMemcpyDeviceToDevice) != cudaSuccess)) {
+            set_error("autotune backup of the low part failed");
+            rc = DGX_ERR_NOMEM;
+            break;
+        }
         if (cudaMemcpy(saved[i], s.c, bytes, cudaMemcpyDeviceToDevice) != cudaSuccess ||
             cudaMemcpy(&scal[8 * i], s.scal, 8 * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
             cudaMemcpy(&steps[i], s.steps, sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess)
@@ -676,6 +684,10 @@ int dgx_batch_autotune(dgx_batch *b, int reps, void *stream) {
         SolverDev &s = b->solvers[i]->s;
         if (!saved[i]) continue;
         const size_t bytes = s.n * (s.precision == DGX_FP64 ? 8 : 4);
+        if (saved_lo[i]) {
+            if (cudaMemcpy(s.lo, saved_lo[i], bytes, cudaMemcpyDeviceToDevice) != cudaSuccess) rc = rc ? rc : DGX_ERR_CUDA;
+            cudaFree(saved_lo[i]);
+        }
         if (cudaMemcpy(s.c, saved[i], bytes, cudaMemcpyDeviceToDevice) != cudaSuccess ||
             cudaMemcpy(s.scal, &scal[8 * i], 8 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemcpy(s.steps, &steps[i], sizeof(long long), cudaMemcpyHostToDevice) != cudaSuccess)

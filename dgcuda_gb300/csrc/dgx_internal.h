@@ -162,6 +162,7 @@ struct SolverDev {
     void *c = nullptr;                 // resident state (FP32 or FP64)
     void *acc = nullptr;               // RK4 accumulator (RK4 only)
     void *ua = nullptr, *ub = nullptr; // stage inputs (ub: RK4 only)
+    void *lo = nullptr;                // DGX_FP32_COMP: the state's low part (state = c + lo)
     // device scalars: [0] dt of the current step, [1] t at the end of it,
     // [2] t at its start, [3] fixed dt, [4] cfl, [5] t_end, [6] max wave speed
     double *scal = nullptr;
@@ -226,6 +227,11 @@ struct StageArgs {
     // stage states after they are written)
     const void *aux;
     int rk13;
+    // compensated RK4 (DGX_FP32_COMP, comp = 1): acc holds the increment
+    // accumulator D and aux the state's low part lo (state = c + lo):
+    //   1 u2 = c + k1/2, D = lo + k1/6;  2/3 u = c + alpha k, D += k/3;
+    //   4 (c, lo) = two-sum(c, D + k4/6)
+    int comp;
     const int *nbr;
     const int *halo_off;
     const int *halo_list;

@@ -64,7 +64,8 @@ size_t solver_estimate(const dgx_request &r) {
     const size_t E = 2 * static_cast<size_t>(r.n) * r.n;
     const size_t np = static_cast<size_t>(num_modes(r.order)), nv = r.equation == DGX_EULER ? 4 : 1;
     const size_t vb = r.precision == DGX_FP64 ? 8 : 4;
-    return BlockPool::size_class(4 * (nv * np * E * vb + 64 + 256) + 256);
+    const size_t nvec = r.precision == DGX_FP32_COMP ? 5 : 4;   // c, ua, ub, acc (+ lo)
+    return BlockPool::size_class(nvec * (nv * np * E * vb + 64 + 256) + 256);
 }
 
 }  // namespace
@@ -121,7 +122,7 @@ int validate(const dgx_request &r) {
     if (r.n < 1 || r.n > 8192) return DGX_ERR_INVALID;
     if (r.order < 0 || r.order > kMaxOrder) return DGX_ERR_UNSUPPORTED;
     if (r.equation != DGX_ADVECTION && r.equation != DGX_EULER) return DGX_ERR_INVALID;
-    if (r.precision != DGX_FP32 && r.precision != DGX_FP64) return DGX_ERR_UNSUPPORTED;
+    if (r.precision != DGX_FP32 && r.precision != DGX_FP64 && r.precision != DGX_FP32_COMP) return DGX_ERR_UNSUPPORTED;
     if (!(r.t_end > 0.0) || !(r.lx > 0.0) || !(r.ly > 0.0)) return DGX_ERR_INVALID;
     if (r.dt <= 0.0 && !(r.cfl > 0.0)) return DGX_ERR_INVALID;
     return DGX_OK;

@@ -356,7 +356,7 @@ __device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, uns
     constexpr int NP = num_modes(P);
     const int E = a.E;
     const size_t SE = static_cast<unsigned>(E);   // zero-extended: plane offsets k*SE are 32x32-bit products
-    const bool pre = a.prefetch && a.mode >= 2 && a.mode <= 4;
+    const bool pre = a.prefetch && ((a.mode >= 2 && a.mode <= 4) || (a.comp && a.mode == 1));
     if (pre && tid < 32) {
         // order this CTA's earlier generic-proxy accesses of the shared memory
         // (a previous tile) before the bulk copies that overwrite it
@@ -366,8 +366,10 @@ __device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, uns
         // mode 2 and 3: the base state, then the accumulator (13-pass RK4: mode
         // 2 the base state alone, mode 3 the base state and u2); mode 4: the
         // accumulator
-        const bool base_only = a.rk13 && a.mode == 2;
-        const int ncopy = (a.mode == 4 || base_only) ? nplanes : 2 * nplanes;
+        // compensated RK4: mode 1 the state's low part, modes 2-4 the base
+        // state and the increment accumulator
+        const bool base_only = (a.rk13 && a.mode == 2) || (a.comp && a.mode == 1);
+        const int ncopy = ((a.mode == 4 && !a.comp) || base_only) ? nplanes : 2 * nplanes;
         // plane pl's slice [g0, g0 + cnt) widened to [g0 & -A, (g0 + cnt + A-1) & -A)
         // (the state buffers carry 16 bytes of slack past their end)
         const size_t A = kPreAlign;
@@ -384,12 +386,13 @@ __device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, uns
             // planes [0, nplanes): base state (modes 2, 3), then the accumulator
             // (13-pass mode 3: u2); mode 4 copies only the accumulator, to
             // planes [0, nplanes)
-            const int which = (a.mode == 4) ? 1 : (q >= nplanes);
+            const int which = (a.mode == 4 && !a.comp) ? 1 : (q >= nplanes);
             const int pl = q % nplanes;
             const size_t g0 = pl * SE + static_cast<size_t>(tile) * kTile;
             const size_t a0 = g0 & ~(A - 1), a1 = (g0 + cnt + A - 1) & ~(A - 1);
             const void *second = (a.rk13 && a.mode == 3) ? a.aux : static_cast<const void *>(a.acc);
-            const R *src = static_cast<const R *>(which ? second : a.c) + a0;
+            const void *first = (a.comp && a.mode == 1) ? a.aux : a.c;
+            const R *src = static_cast<const R *>(which ? second : first) + a0;
             bulk_copy_g2s(s_pre + static_cast<size_t>(q) * a.prefetch, src, static_cast<unsigned>((a1 - a0) * sizeof(R)),
                           bar);
         }
@@ -444,11 +447,11 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
         const bool from_u2 = a.rk13 && a.mode == 3;
         const R *pc, *pacc;
         if constexpr (K == 0) {
-            pc = static_cast<const R *>(a.c) + e;
+            pc = static_cast<const R *>((a.comp && a.mode == 1) ? a.aux : a.c) + e;
             pacc = static_cast<const R *>(from_u2 ? a.aux : static_cast<const void *>(a.acc)) + e;
         } else {
             pc = s_pre + row;
-            pacc = s_pre + (a.mode == 4 ? 0 : NV * NP * a.prefetch) + row;
+            pacc = s_pre + ((a.mode == 4 && !a.comp) ? 0 : NV * NP * a.prefetch) + row;
         }
         const int pstride = a.prefetch, sm = static_cast<int>(SE & (kPreAlign - 1));
         auto at = [&](const R *p, int pi) -> R {
@@ -456,7 +459,51 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
             else if constexpr (K == 1) return p[pi * pstride + ((pi * sm) & (kPreAlign - 1))];
             else return p[pi * SE];
         };
-        if (a.mode == 4) {   // c = acc + k4/6
+        if (a.comp) {
+            // compensated RK4 (pc: the state's low part in mode 1, else the
+            // base state; pacc: the increment accumulator D)
+            R *__restrict__ ae = static_cast<R *>(a.acc) + e;
+            if (a.mode == 1) {          // u2 = c + k1/2, D = lo + k1/6
+#pragma unroll
+                for (int n = 0; n < VC; ++n)
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) {
+                        const int pi = (V0 + n) * NP + i;
+                        const R kk = sc * rhs[n][i];
+                        oe[pi * SE] = fma(R(0.5), kk, c[n][i]);
+                        ae[pi * SE] = fma(R(1.0 / 6.0), kk, at(pc, pi));
+                    }
+            } else if (a.mode == 4) {   // (c, lo) = two-sum(c, D + k4/6)
+                // c is read and written in place (each thread its own values,
+                // no other thread reads them in this stage): plain pointers
+                R *oc = static_cast<R *>(a.out) + e;
+                R *ol = static_cast<R *>(const_cast<void *>(a.aux)) + e;
+#pragma unroll
+                for (int n = 0; n < VC; ++n)
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) {
+                        const int pi = (V0 + n) * NP + i;
+                        const R y = fma(R(1.0 / 6.0), sc * rhs[n][i], at(pacc, pi));
+                        const R b = at(pc, pi);
+                        const R t = b + y;   // the two-sum (Knuth): t + err = b + y exactly
+                        const R bp = t - b;
+                        const R err = (b - (t - bp)) + (y - bp);
+                        oc[pi * SE] = t;
+                        ol[pi * SE] = err;
+                    }
+            } else {                    // 2, 3: u = c + alpha k, D += k/3
+                const R alpha = a.mode == 2 ? R(0.5) : R(1);
+#pragma unroll
+                for (int n = 0; n < VC; ++n)
+#pragma unroll
+                    for (int i = 0; i < NP; ++i) {
+                        const int pi = (V0 + n) * NP + i;
+                        const R kk = sc * rhs[n][i];
+                        oe[pi * SE] = fma(alpha, kk, at(pc, pi));
+                        ae[pi * SE] = fma(R(1.0 / 3.0), kk, at(pacc, pi));
+                    }
+            }
+        } else if (a.mode == 4) {   // c = acc + k4/6
 #pragma unroll
             for (int n = 0; n < VC; ++n)
 #pragma unroll
@@ -520,6 +567,12 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
             for (int i = 0; i < NP; ++i) out[((V0 + n) * NP + i) * SE + e] = sc * rhs[n][i];
         break;
     case 1: {   // u2 = c + k1/2, and in the 16-pass form acc = c + k1/6
+        if (a.comp) {   // and D = lo + k1/6 (rk_tail)
+            if (!pre) rk_tail(IntC<0>{});
+            else if (a.prefetch == kTile) rk_tail(IntC<2>{});
+            else rk_tail(IntC<1>{});
+            break;
+        }
         R *__restrict__ ae = static_cast<R *>(a.acc) + e;
         if (a.rk13) {
 #pragma unroll

@@ -45,7 +45,21 @@ enum dgx_status {
 
 enum dgx_equation { DGX_ADVECTION = 0, DGX_EULER = 1 };
 enum dgx_flux { DGX_FLUX_CENTRAL = 0, DGX_FLUX_LLF = 1 };
-enum dgx_precision { DGX_FP32 = 0, DGX_FP32_BF16X3 = 1, DGX_FP64 = 2 };
+/* Precisions:
+ *   FP32         FP32 state and arithmetic (the plain path).
+ *   FP32_BF16X3  FP32 state, the basis contractions on the tensor cores.
+ *   FP64         the reference's precision.
+ *   FP32_COMP    FP32 state and arithmetic, RK4 only, with compensated
+ *                accumulation: the stage increments k1/6 + k2/3 + k3/3 are
+ *                accumulated apart from the state, and the state is carried as
+ *                a pair (c, lo) of FP32 arrays whose sum is updated by an
+ *                error-free two-sum each step.  Its rounding then stays near
+ *                1e-7 over thousands of steps, where FP32 storage alone
+ *                accumulates ~1e-5 (the FP32 rounding of the stored state, not
+ *                the FP32 arithmetic, sets that error).  One more state vector
+ *                on the device and 19 state passes per RK4 step instead of 13.
+ *                No counterpart in the reference (FP64 throughout). */
+enum dgx_precision { DGX_FP32 = 0, DGX_FP32_BF16X3 = 1, DGX_FP64 = 2, DGX_FP32_COMP = 3 };
 /* Time integrators (src/2d/conservation/time_integrator.cu):
  *   RK4  classic four-stage Runge-Kutta (time_integrate_rk4, :221-434)
  *   RK2  explicit midpoint: c += k(c + k(c)/2) (time_integrate_rk2, :466-614)
