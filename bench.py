@@ -410,9 +410,9 @@ def run_batched(steps: int = 20):
 
 def _batched_compensated(specs, steps):
     """The batched configuration in the compensated FP32 precision
-    (DGX_FP32_COMP): the same solves one by one and batched (per-class
-    launches, default options), 2 x (3 + steps) steps in all, then the same
-    accuracy sample against the FP64 path as the FP32 run."""
+    (DGX_FP32_COMP): the same solves one by one and batched (autotuned),
+    2 x (3 + steps) steps in all, then the same accuracy sample against the
+    FP64 path as the FP32 run."""
     import torch
     from dgcuda_gb300 import _ffi
     from dgcuda_gb300.batch import Batch
@@ -434,6 +434,7 @@ def _batched_compensated(specs, steps):
         torch.cuda.synchronize()
         plain_ms = a.elapsed_time(b) / steps
         bt = Batch(solvers)
+        bt.autotune(reps=2, stream=sh)   # restores the solves' states and times
         for _ in range(3):
             bt.step(sh)
         torch.cuda.synchronize()
@@ -443,6 +444,7 @@ def _batched_compensated(specs, steps):
         b.record(stream)
         torch.cuda.synchronize()
         batch_ms = a.elapsed_time(b) / steps
+        mode = bt.fused()[0]
     bt.close()
     accuracy = _sample_accuracy(specs, solvers, 2 * (3 + steps))
     for sv in solvers:
@@ -450,7 +452,9 @@ def _batched_compensated(specs, steps):
     return {"precision": "fp32_comp (compensated accumulation of the RK4 increments)",
             "value": dofs / (batch_ms * 1e-3), "ms_per_step": batch_ms,
             "plain_value": dofs / (plain_ms * 1e-3), "plain_ms_per_step": plain_ms,
-            "speedup_vs_plain": plain_ms / batch_ms, "accuracy": accuracy, "unit": UNIT}
+            "speedup_vs_plain": plain_ms / batch_ms,
+            "launch_mode": {0: "per_class", 2: "fused_2cta", 3: "fused_3cta"}[mode],
+            "accuracy": accuracy, "unit": UNIT}
 
 
 def _sample_accuracy(specs, solvers, nsteps, every: int = 16, states=None):
