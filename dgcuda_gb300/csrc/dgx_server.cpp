@@ -6,9 +6,12 @@
 // while the device-memory budget and the slot limit allow.  It creates their
 // solvers, whose state then stays resident on the device, and repacks the
 // active set into a batch (per-class work lists + a CUDA-graph step) whenever
-// solves join or finish.  It then advances the batch a few steps at a time,
-// gathers every solve's time in one copy, and retires the solves that reached
-// their end time, recording time-to-solution.  Requests that arrive while
+// solves join or finish.  It advances the batch a few steps at a time, and
+// while the GPU runs those steps it admits the next requests (their meshes
+// are generated and checked on the host meanwhile; their uploads and
+// projections queue behind the steps); then it gathers every solve's time in
+// one copy, and retires the solves that reached their end time, recording
+// time-to-solution.  Requests that arrive while
 // others run join at the next repack, so their work overlaps on the device.
 // Each solve's result is the same alone and in the mix (the batched kernels are
 // bitwise equal to the plain path).
@@ -321,8 +324,8 @@ void worker_main(dgx_server *s) {
     std::vector<double> t, dt;
     std::vector<unsigned int> st;
     std::vector<long long> stp;
+    bool repack = false;   // the active set changed since the batch was built
     for (;;) {
-        bool changed = false;
         std::vector<Request *> admit;
         {
             std::unique_lock<std::mutex> lk(s->mu);
@@ -360,10 +363,43 @@ void worker_main(dgx_server *s) {
                 s->in_transit++;
             }
         }
-        const auto ta = Clock::now();
+        // (1) the running solves' next steps go on the stream first, so that
+        // the admission round's host work (mesh generation and checks) below
+        // runs while the GPU steps; its uploads and projections queue behind
+        // the steps on the same stream
+        const auto tp = Clock::now();
+        auto tb = tp;   // when the steps were queued
+        bool stepped = false;
+        if (!s->active.empty()) {
+            if (repack || !s->batch) {
+                if (s->batch) dgx_batch_destroy(s->batch);
+                s->batch = nullptr;
+                std::vector<dgx_solver *> sv;
+                for (Request *q : s->active) sv.push_back(q->solver);
+                int rc = dgx_batch_create(sv.data(), static_cast<int>(sv.size()), &s->batch);
+                s->repacks++;
+                repack = false;
+                if (rc) {
+                    std::lock_guard<std::mutex> lk(s->mu);
+                    for (Request *q : s->active) { release_solve(s, q); finish(s, q, kFailed, rc); }
+                    s->active.clear();
+                }
+            }
+            if (s->batch) {
+                tb = Clock::now();
+                {
+                    std::lock_guard<std::mutex> lk(s->mu);
+                    s->repack_s += std::chrono::duration<double>(tb - tp).count();
+                }
+                dgx_batch_run(s->batch, s->steps_per_check, s->stream);
+                stepped = true;
+            }
+        }
+        const auto t0 = Clock::now();
+        // (2) the admission round
         std::vector<Request *> started;
         std::vector<std::pair<dgx_mesh *, size_t>> fresh;
-        s->stage_off = 0;   // the stream is idle between rounds
+        s->stage_off = 0;   // the previous round's uploads have completed
         if (admit.size() > s->min_diam_cap) {
             if (s->min_diam) cudaFreeHost(s->min_diam);
             s->min_diam = nullptr;
@@ -382,92 +418,58 @@ void worker_main(dgx_server *s) {
             release_solve(s, q);
             finish(s, q, kFailed, rc);
         }
+        cudaError_t admit_err = cudaSuccess;
+        if (!admit.empty()) {   // the host's part of the round (the GPU meanwhile runs the steps)
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->admit_s += std::chrono::duration<double>(Clock::now() - t0).count();
+        }
         if (!started.empty() || !fresh.empty()) {
-            // one synchronisation for the whole admission round: the uploads and
-            // projections have run (and any fault of theirs shows here)
-            const cudaError_t ce = cudaStreamSynchronize(s->stream);
+            // one synchronisation for the whole admission round (and the steps
+            // queued before it): the uploads and projections have run, and any
+            // fault of theirs shows here
+            admit_err = cudaStreamSynchronize(s->stream);
             for (auto &f : fresh) f.first->d.min_diam = s->min_diam[f.second];
-            std::lock_guard<std::mutex> lk(s->mu);
-            for (Request *q : started) {
-                s->in_transit--;
-                if (ce != cudaSuccess) {
-                    release_solve(s, q);
-                    finish(s, q, kFailed, DGX_ERR_CUDA);
-                    continue;
-                }
-                q->state = kRunning;
-                q->started = Clock::now();
-                s->active.push_back(q);
-                changed = true;
-            }
         }
-        const auto tr = Clock::now();
-        if (!admit.empty()) {
-            std::lock_guard<std::mutex> lk(s->mu);
-            s->admit_s += std::chrono::duration<double>(tr - ta).count();
-        }
-        if (s->active.empty()) continue;
-        // repack the active set into one batch
-        if (changed || !s->batch) {
-            if (s->batch) dgx_batch_destroy(s->batch);
-            s->batch = nullptr;
-            std::vector<dgx_solver *> sv;
-            for (Request *q : s->active) sv.push_back(q->solver);
-            int rc = dgx_batch_create(sv.data(), static_cast<int>(sv.size()), &s->batch);
-            s->repacks++;
-            if (rc) {
+        // (3) the steps' progress: finished solves read back and released
+        if (stepped) {
+            const size_t n = s->active.size();
+            t.resize(n); dt.resize(n); st.resize(n); stp.resize(n);
+            int rc = dgx_batch_progress(s->batch, t.data(), dt.data(), st.data(), stp.data(), s->stream);
+            if (s->stall_seconds > 0.0)   // host-side fault injection: a stalled worker
+                std::this_thread::sleep_for(std::chrono::duration<double>(s->stall_seconds));
+            const auto t1 = Clock::now();
+            std::vector<Request *> keep, done, leaving;
+            std::vector<double> t_done;
+            {
                 std::lock_guard<std::mutex> lk(s->mu);
-                for (Request *q : s->active) { release_solve(s, q); finish(s, q, kFailed, rc); }
-                s->active.clear();
-                continue;
-            }
-        }
-        const auto t0 = Clock::now();
-        if (t0 > tr) {
-            std::lock_guard<std::mutex> lk(s->mu);
-            s->repack_s += std::chrono::duration<double>(t0 - tr).count();
-        }
-        dgx_batch_run(s->batch, s->steps_per_check, s->stream);
-        const size_t n = s->active.size();
-        t.resize(n); dt.resize(n); st.resize(n); stp.resize(n);
-        int rc = dgx_batch_progress(s->batch, t.data(), dt.data(), st.data(), stp.data(), s->stream);
-        if (s->stall_seconds > 0.0)   // host-side fault injection: a stalled worker
-            std::this_thread::sleep_for(std::chrono::duration<double>(s->stall_seconds));
-        const auto t1 = Clock::now();
-        // finished solves: totals (and kept states) read back, then released
-        std::vector<Request *> keep, done, leaving;
-        std::vector<double> t_done;
-        {
-            std::lock_guard<std::mutex> lk(s->mu);
-            s->busy += std::chrono::duration<double>(t1 - t0).count();
-            s->steps += s->steps_per_check;
-            for (size_t i = 0; i < n; ++i) {
-                Request *q = s->active[i];
-                const long long done_steps = rc == DGX_OK ? stp[i] : q->steps;
-                s->dof_updates += static_cast<double>(done_steps - q->steps) * q->dofs;
-                q->steps = done_steps;
-                const bool bad = rc != DGX_OK || st[i] != 0;
-                const bool fin = !bad && (t[i] >= q->r.t_end || dt[i] == 0.0);
-                if (fin) {
-                    done.push_back(q);
-                    t_done.push_back(t[i]);
-                } else if (bad || q->cancel) {
-                    leaving.push_back(q);
-                } else {
-                    keep.push_back(q);
+                s->busy += std::chrono::duration<double>(t1 - tb).count();
+                s->steps += s->steps_per_check;
+                for (size_t i = 0; i < n; ++i) {
+                    Request *q = s->active[i];
+                    const long long done_steps = rc == DGX_OK ? stp[i] : q->steps;
+                    s->dof_updates += static_cast<double>(done_steps - q->steps) * q->dofs;
+                    q->steps = done_steps;
+                    const bool bad = rc != DGX_OK || st[i] != 0;
+                    const bool fin = !bad && (t[i] >= q->r.t_end || dt[i] == 0.0);
+                    if (fin) {
+                        done.push_back(q);
+                        t_done.push_back(t[i]);
+                    } else if (bad || q->cancel) {
+                        leaving.push_back(q);
+                    } else {
+                        keep.push_back(q);
+                    }
                 }
             }
-        }
-        const int trc = retire_totals(s, done);
-        for (size_t j = 0; j < done.size() && !trc; ++j) {
-            Request *q = done[j];
-            q->t_final = t_done[j];
-            if (q->r.keep_state) {
-                q->result.resize(q->solver->s.n);
-                dgx_get_state(q->solver, q->result.data());
+            const int trc = retire_totals(s, done);
+            for (size_t j = 0; j < done.size() && !trc; ++j) {
+                Request *q = done[j];
+                q->t_final = t_done[j];
+                if (q->r.keep_state) {
+                    q->result.resize(q->solver->s.n);
+                    dgx_get_state(q->solver, q->result.data());
+                }
             }
-        }
-        {
             std::lock_guard<std::mutex> lk(s->mu);
             for (Request *q : done) {
                 release_solve(s, q);
@@ -483,9 +485,26 @@ void worker_main(dgx_server *s) {
                 s->active.swap(keep);
                 if (s->batch) dgx_batch_destroy(s->batch);
                 s->batch = nullptr;
+                repack = true;
                 evict_idle_meshes(s, 0, kIdleMeshes, std::set<MeshKey>());
             }
             s->retire_s += std::chrono::duration<double>(Clock::now() - t1).count();
+        }
+        // (4) the admitted solves join the active set; the next round repacks
+        if (!started.empty()) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            for (Request *q : started) {
+                s->in_transit--;
+                if (admit_err != cudaSuccess) {
+                    release_solve(s, q);
+                    finish(s, q, kFailed, DGX_ERR_CUDA);
+                    continue;
+                }
+                q->state = kRunning;
+                q->started = Clock::now();
+                s->active.push_back(q);
+                repack = true;
+            }
         }
     }
     if (s->batch) dgx_batch_destroy(s->batch);

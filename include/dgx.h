@@ -409,10 +409,13 @@ enum dgx_request_state { DGX_REQ_QUEUED = 0, DGX_REQ_RUNNING = 1, DGX_REQ_DONE =
 typedef struct dgx_server_stats {
     long long submitted, completed, failed, active, queued, repacks, steps;
     double dof_updates;          /* DOF-updates performed by completed and running solves */
-    double busy_seconds;         /* worker time spent stepping                          */
+    double busy_seconds;         /* worker time from queueing a round of steps to reading
+                                    their progress (the admission work of the round,
+                                    which overlaps the steps on the GPU, included)      */
     double p50_latency_s, p99_latency_s, max_latency_s;   /* time-to-solution           */
     size_t device_bytes_in_use;  /* admitted footprint                                  */
-    double admit_seconds;        /* worker time spent creating admitted solves          */
+    double admit_seconds;        /* worker time spent creating admitted solves (while
+                                    the GPU runs the steps queued before them)           */
     double repack_seconds;       /* worker time spent rebuilding the batch              */
     double retire_seconds;       /* worker time spent reading out and freeing finished solves */
     double idle_seconds;         /* worker time spent waiting for requests              */
