@@ -225,7 +225,7 @@ struct StageArgs {
     // input u3 = c + k2/2; rk13 = 0: the 16-pass form with the accumulator
     // written by every stage (kept for the per-stage limiter, which changes the
     // stage states after they are written)
-    const void *aux;
+    void *aux;         // read in 13-pass mode 3 and compensated mode 1, written in compensated mode 4
     int rk13;
     // compensated RK4 (DGX_FP32_COMP, comp = 1): acc holds the increment
     // accumulator D and aux the state's low part lo (state = c + lo):

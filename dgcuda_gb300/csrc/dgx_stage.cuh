@@ -390,7 +390,7 @@ __device__ __forceinline__ bool issue_prefetch(const StageArgs &a, int tile, uns
             const int pl = q % nplanes;
             const size_t g0 = pl * SE + static_cast<size_t>(tile) * kTile;
             const size_t a0 = g0 & ~(A - 1), a1 = (g0 + cnt + A - 1) & ~(A - 1);
-            const void *second = (a.rk13 && a.mode == 3) ? a.aux : static_cast<const void *>(a.acc);
+            const void *second = (a.rk13 && a.mode == 3) ? a.aux : a.acc;
             const void *first = (a.comp && a.mode == 1) ? a.aux : a.c;
             const R *src = static_cast<const R *>(which ? second : first) + a0;
             bulk_copy_g2s(s_pre + static_cast<size_t>(q) * a.prefetch, src, static_cast<unsigned>((a1 - a0) * sizeof(R)),
@@ -448,7 +448,7 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
         const R *pc, *pacc;
         if constexpr (K == 0) {
             pc = static_cast<const R *>((a.comp && a.mode == 1) ? a.aux : a.c) + e;
-            pacc = static_cast<const R *>(from_u2 ? a.aux : static_cast<const void *>(a.acc)) + e;
+            pacc = static_cast<const R *>(from_u2 ? a.aux : a.acc) + e;
         } else {
             pc = s_pre + row;
             pacc = s_pre + ((a.mode == 4 && !a.comp) ? 0 : NV * NP * a.prefetch) + row;
@@ -477,7 +477,7 @@ __device__ __forceinline__ bool stage_epilogue(const StageArgs &a, const R (&rhs
                 // c is read and written in place (each thread its own values,
                 // no other thread reads them in this stage): plain pointers
                 R *oc = static_cast<R *>(a.out) + e;
-                R *ol = static_cast<R *>(const_cast<void *>(a.aux)) + e;
+                R *ol = static_cast<R *>(a.aux) + e;
 #pragma unroll
                 for (int n = 0; n < VC; ++n)
 #pragma unroll
