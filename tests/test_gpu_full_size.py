@@ -10,8 +10,8 @@ the C ABI) against the FP64 CPU oracle run on the same inputs:
 
 Tolerances (relative L2 per conserved variable against the oracle): config 3
 FP32 <= 1e-5 with conserved-total drift <= 1e-6 relative; config 2 FP64
-<= 1e-9 and FP32 <= 3e-4 (its ~1,630 steps accumulate FP32 rounding, see the
-test).  The oracle takes about ten seconds (config 2) and three minutes
+<= 1e-9, FP32 <= 3e-4 (its ~1,630 steps accumulate the FP32 rounding of the
+stored state, see the test) and compensated FP32 <= 1e-5.  The oracle takes about ten seconds (config 2) and three minutes
 (config 3) on 16 host cores.
 """
 import numpy as np
@@ -32,14 +32,15 @@ WAVE = (0.2, 1.0, 1.0, 1.0, 1.0)
 
 def test_config2_vortex_full_size(gpu, oracle_mod):
     """About 1,630 CFL steps.  The FP64 path matches the oracle to 1e-9.  The
-    FP32 path's rounding accumulates over so long a run: measured on GB300
-    2.7e-5 / 4.3e-5 / 1.4e-4 / 1.8e-5 (rho, rho u, rho v, E) against the
-    oracle, largest for rho v, whose free-stream value is 0 while its flux
-    carries the O(1) pressure (the element's volume and side terms cancel to
-    the net RHS, and the FP32 rounding of those terms recurs every step).  The
-    1e-5 bound of the FP32 path holds for runs of the benchmark's length
-    (config 3, 100 steps, below); a run of this length at that accuracy takes
-    the FP64 path.  Bounds: FP64 <= 1e-9; FP32 <= 3e-4."""
+    plain FP32 path's rounding accumulates over so long a run: measured on
+    GB300 2.7e-5 / 4.3e-5 / 1.4e-4 / 1.8e-5 (rho, rho u, rho v, E) against the
+    oracle, largest for rho v, whose free-stream value is 0.  The source is the
+    FP32 rounding of the stored state that the RK4 sum accumulates, step after
+    step (an FP64 run with its stored stage outputs rounded to FP32 shows the
+    same error; with only the right-hand sides' inputs rounded, 1e-7), so the
+    compensated FP32 precision, which keeps the increments apart from the
+    state and the state as c + lo, holds this run to 1e-5.  Bounds: FP64
+    <= 1e-9; FP32 <= 3e-4; compensated FP32 <= 1e-5."""
     orc = oracle_mod
     m = periodic_square(128, lx=10.0, ly=10.0, jitter=0.15, seed=12347)
     o = orc.Oracle(m, 2, orc.EULER, orc.LLF)
@@ -51,7 +52,8 @@ def test_config2_vortex_full_size(gpu, oracle_mod):
     e_orc = orc.rel_l2(ref, exact)
     # the discretisation error of the scheme: 2e-6 .. 1.5e-5 per variable
     assert e_orc.max() <= 2e-5, e_orc
-    for precision, tol in ((_ffi.FP64, 1e-9), (_ffi.FP32, 3e-4)):
+    names = {_ffi.FP64: "fp64", _ffi.FP32: "fp32", _ffi.FP32_COMP: "fp32 compensated"}
+    for precision, tol in ((_ffi.FP64, 1e-9), (_ffi.FP32, 3e-4), (_ffi.FP32_COMP, 1e-5)):
         sv = Solver(m, 2, _ffi.EULER, _ffi.FLUX_LLF, precision)
         sv.set_state(c0)
         sv.set_dt(None)
@@ -60,7 +62,7 @@ def test_config2_vortex_full_size(gpu, oracle_mod):
         sv.close()
         assert n == nref and abs(t - 2.0) < 1e-12
         err = orc.rel_l2(got, ref)
-        print(f"config 2 {'fp64' if precision == _ffi.FP64 else 'fp32'}: {n} steps, rel L2 vs oracle {err}, "
+        print(f"config 2 {names[precision]}: {n} steps, rel L2 vs oracle {err}, "
               f"vs exact {orc.rel_l2(got, exact)} (oracle vs exact {e_orc})")
         assert err.max() <= tol, err
 

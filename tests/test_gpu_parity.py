@@ -3,6 +3,7 @@ reference's own outputs (golden vectors).
 
 Tolerances (relative L2 per conserved variable):
   states (after RK4 steps / runs), FP32 path vs FP64 oracle     <= 1e-5
+    (the compensated FP32 precision too: over 10-20 steps it gains little)
   states, FP64 path vs FP64 oracle                              <= 1e-11
   one RHS, FP64 path vs FP64 oracle                             <= 1e-12
   one RHS, FP32 path vs FP64 oracle on the same FP32 input      <= 5e-5
