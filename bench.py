@@ -820,7 +820,7 @@ def run_ours(args, rank, world, local):
     n = args.mesh_n
     mesh = build_mesh(n)
     E = mesh.num_elem
-    prec = _ffi.FP32_BF16X3 if args.precision == "bf16x3" else _ffi.FP32
+    prec = {"bf16x3": _ffi.FP32_BF16X3, "fp32comp": _ffi.FP32_COMP}.get(args.precision, _ffi.FP32)
     sv = density_wave_solver(mesh, prec)
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
@@ -836,6 +836,9 @@ def run_ours(args, rank, world, local):
     stage_bytes = (13 * X + 3 * G) / 3.0          # per timed stage 2-4 launch (average; stage 1 is timed with the CFL kernel)
     moved_step_bytes = 13 * X + 4 * G
     moved_stage_bytes = (11 * X + 3 * G) / 3.0
+    if prec == _ffi.FP32_COMP:   # the compensated form: stages 4X+G, 5X+G, 5X+G, 5X+G
+        moved_step_bytes = 19 * X + 4 * G
+        moved_stage_bytes = 5 * X + G
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -870,8 +873,9 @@ def run_ours(args, rank, world, local):
     peak, peak_src = peaks()
     achieved = stage_bytes / (stage_ms * 1e-3) / 1e9
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "stage_kernel_density_wave_p3.json" if prec == _ffi.FP32
-                        else "stage_kernel_tc_density_wave_p3.json")
+    prof = os.path.join(ROOT, "profiles", {_ffi.FP32: "stage_kernel_density_wave_p3.json",
+                                           _ffi.FP32_BF16X3: "stage_kernel_tc_density_wave_p3.json",
+                                           _ffi.FP32_COMP: "stage_kernel_comp_density_wave_p3.json"}[prec])
     if os.path.exists(prof) and n == 1024:
         try:
             traffic = json.load(open(prof)).get("dram_bytes_per_launch")
@@ -885,8 +889,9 @@ def run_ours(args, rank, world, local):
                        parallelism="replicas" if world > 1 else "single"),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": ("stage_kernel_tc<3,EULER> (fused RK4 stage, BF16x3 MMA)" if prec != _ffi.FP32
-                                else "stage_kernel<3,EULER> (fused RK4 stage, FP32)"),
+                     "kernel": {_ffi.FP32_BF16X3: "stage_kernel_tc<3,EULER> (fused RK4 stage, BF16x3 MMA)",
+                                _ffi.FP32_COMP: "stage_kernel<3,EULER> (fused RK4 stage, FP32, compensated)"}.get(
+                                    prec, "stage_kernel<3,EULER> (fused RK4 stage, FP32)"),
                      "algorithmic_bytes_per_launch": stage_bytes,
                      "algorithmic_bytes_per_step": step_bytes,
                      "step_achieved": step_bytes / (ms_step * 1e-3) / 1e9,
@@ -923,9 +928,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mesh-n", type=int, default=1024)
-    ap.add_argument("--precision", choices=["fp32", "bf16x3"], default="fp32",
-                    help="arithmetic of the timed path: plain FP32, or FP32 with the basis "
-                         "contractions on the tensor cores (BF16x3)")
+    ap.add_argument("--precision", choices=["fp32", "bf16x3", "fp32comp"], default="fp32",
+                    help="arithmetic of the timed path: plain FP32, FP32 with the basis "
+                         "contractions on the tensor cores (BF16x3), or FP32 with compensated "
+                         "RK4 accumulation")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the batched and served sections")
     ap.add_argument("--only", choices=["batched", "served", "served_stated"], default=None,
