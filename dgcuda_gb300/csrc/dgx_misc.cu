@@ -119,11 +119,17 @@ __global__ void reduce_kernel(const double *x, size_t n, double *partial, double
     if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
 }
 
-// per-element products c_{n,0,e} * J_e for the conserved totals
+// per-element products c_{n,0,e} * J_e for the conserved totals; lo (the
+// compensated precision's low part of the state, or null) is added to c first
 template <typename T>
-__global__ void mass_terms_kernel(const T *c, const double *J, int E, int np, int n, double *out) {
+__global__ void mass_terms_kernel(const T *c, const T *lo, const double *J, int E, int np, int n, double *out) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < E) out[e] = static_cast<double>(c[static_cast<size_t>(n) * np * E + e]) * J[e];
+    if (e < E) {
+        const size_t i = static_cast<size_t>(n) * np * E + e;
+        double v = static_cast<double>(c[i]);
+        if (lo) v += static_cast<double>(lo[i]);
+        out[e] = v * J[e];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -406,10 +412,10 @@ int conserved_totals(SolverDev &s, const MeshDev &m, double *out, cudaStream_t s
     for (int n = 0; n < s.nv && rc == DGX_OK; ++n) {
         if (s.precision == DGX_FP64)
             mass_terms_kernel<double><<<blocks_for(E), kThreads, 0, st>>>(
-                static_cast<const double *>(s.c), m.J, E, s.np, n, terms);
+                static_cast<const double *>(s.c), nullptr, m.J, E, s.np, n, terms);
         else
             mass_terms_kernel<float><<<blocks_for(E), kThreads, 0, st>>>(
-                static_cast<const float *>(s.c), m.J, E, s.np, n, terms);
+                static_cast<const float *>(s.c), static_cast<const float *>(s.lo), m.J, E, s.np, n, terms);
         if (cudaGetLastError() != cudaSuccess) { rc = DGX_ERR_CUDA; break; }
         double sum = 0.0;
         rc = reduce_host(terms, E, 0, scratch, len, &sum, st);
@@ -439,10 +445,10 @@ int conserved_sums_async(const SolverDev &s, const MeshDev &m, double *terms, do
     for (int n = 0; n < s.nv; ++n) {
         if (s.precision == DGX_FP64)
             mass_terms_kernel<double><<<blocks_for(E), kThreads, 0, st>>>(
-                static_cast<const double *>(s.c), m.J, E, s.np, n, terms);
+                static_cast<const double *>(s.c), nullptr, m.J, E, s.np, n, terms);
         else
             mass_terms_kernel<float><<<blocks_for(E), kThreads, 0, st>>>(
-                static_cast<const float *>(s.c), m.J, E, s.np, n, terms);
+                static_cast<const float *>(s.c), static_cast<const float *>(s.lo), m.J, E, s.np, n, terms);
         DGX_CHECK_LAUNCH();
         const int rc = reduce_dev(terms, E, 0, scratch, kReduceLen, dev_sums + n, st);
         if (rc) return rc;

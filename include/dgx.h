@@ -53,12 +53,15 @@ enum dgx_flux { DGX_FLUX_CENTRAL = 0, DGX_FLUX_LLF = 1 };
  *                accumulation: the stage increments k1/6 + k2/3 + k3/3 are
  *                accumulated apart from the state, and the state is carried as
  *                a pair (c, lo) of FP32 arrays whose sum is updated by an
- *                error-free two-sum each step.  Its rounding then stays near
- *                1e-7 over thousands of steps, where FP32 storage alone
- *                accumulates ~1e-5 (the FP32 rounding of the stored state, not
- *                the FP32 arithmetic, sets that error).  One more state vector
- *                on the device and 19 state passes per RK4 step instead of 13.
- *                No counterpart in the reference (FP64 throughout). */
+ *                error-free two-sum each step.  Over thousands of steps it
+ *                stays within ~1e-6 of FP64, where FP32 storage alone
+ *                accumulates 1e-5 .. 1e-4 (the FP32 rounding of the stored
+ *                state, not the FP32 arithmetic, sets that error).  One more
+ *                state vector on the device and 19 state passes per RK4 step
+ *                instead of 13.  dgx_get_state returns c + lo, dgx_set_state
+ *                splits an FP64 state into the pair, dgx_set_state_f32 clears
+ *                lo, dgx_state_device_ptr gives c.  No counterpart in the
+ *                reference (FP64 throughout). */
 enum dgx_precision { DGX_FP32 = 0, DGX_FP32_BF16X3 = 1, DGX_FP64 = 2, DGX_FP32_COMP = 3 };
 /* Time integrators (src/2d/conservation/time_integrator.cu):
  *   RK4  classic four-stage Runge-Kutta (time_integrate_rk4, :221-434)
@@ -209,7 +212,8 @@ int dgx_run(dgx_solver *solver, double t_end, int max_steps, int *steps, double 
 /* Current simulation time and last dt (synchronises the stream). */
 int dgx_time(dgx_solver *solver, double *t, double *dt, void *stream);
 int dgx_reset_time(dgx_solver *solver, double t);
-/* Conserved totals  int u_n dx  in FP64 (deterministic device reduction).
+/* Conserved totals  int u_n dx  in FP64 (deterministic device reduction; in
+ * DGX_FP32_COMP of the state's two parts, c + lo).
  * The first call on a solver allocates its scratch (8 bytes per element plus
  * 32 KiB), kept until the solver is destroyed; later calls allocate nothing.
  * Synchronous (the totals are host doubles). */

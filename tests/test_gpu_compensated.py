@@ -114,6 +114,19 @@ def test_state_pair_holds_fp64_values(gpu):
     sv.close()
 
 
+def test_totals_of_the_state_pair(gpu, oracle_mod):
+    """dgx_conserved_totals of a compensated solver is the total of c + lo:
+    equal to the oracle's totals of the FP64 state set into it."""
+    m = periodic_square(9, lx=10.0, ly=10.0, jitter=0.15, seed=8)
+    sv = Solver(m, 2, _ffi.EULER, _ffi.FLUX_LLF, _ffi.FP32_COMP)
+    o = oracle_mod.Oracle(m, 2, oracle_mod.EULER, oracle_mod.LLF)
+    c = o.project(oracle_mod.IC_VORTEX, (5.0, 5.0, 3.0, 1.0, 0.5, 10.0, 10.0))
+    sv.set_state(c)
+    ref = o.totals(c)
+    np.testing.assert_allclose(sv.totals(), ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+    sv.close()
+
+
 def test_compensated_refuses_other_integrators(gpu):
     m = periodic_square(4)
     with pytest.raises(_ffi.DgxError):
