@@ -246,8 +246,13 @@ def test_config1_advection(gpu, oracle_mod):
     assert n == nref == 1358 and abs(t - 1.0) < 1e-12
     c = sv.get_state()
     assert rel_l2(c, ref).max() <= FP32_TOL
-    # after one period the exact solution is the initial condition
-    assert rel_l2(c, c0).max() < 0.2
+    # after one period the exact solution is the initial condition: the
+    # scheme's own error there (p = 1 on a pulse about two elements wide) is
+    # 5.6 % in the coefficients' L2 norm; the GPU's equals the FP64 oracle's
+    # within the parity bound (|err - err_ref| <= ||c - ref|| / ||c0||)
+    err, err_ref = rel_l2(c, c0).max(), rel_l2(ref, c0).max()
+    assert 0.05 < err_ref < 0.06
+    assert abs(err - err_ref) <= FP32_TOL
 
 
 def test_config2_vortex_reduced(gpu, oracle_mod):
