@@ -10,12 +10,13 @@ baseline/_ref) with `ref_gpu_harness.cu` as their problem file and driver.
 reference's time_integrate_rk4 (src/2d/conservation/time_integrator.cu:221-434),
 or time_integrate_rk2 (:466-614), advance to t_end with its CFL rule: on
 periodic meshes with the harness's own hooks, or with the boundary hooks of the
-reference's cylinder (src/2d/conservation/euler/cylinder/cylinder.cu) or
-supersonic-vortex (euler/supersonic/supersonic.cu) problem file, compiled in
-(`problem`); `run_advection` lets the advection solver's
-time_integrate_rk4 (src/2d/time_integrator.cu:89-315) take a number of steps of
-a fixed dt (a = (1,1), central flux).  Both return the state, the steps taken
-and the time.
+reference's cylinder (src/2d/conservation/euler/cylinder/cylinder.cu),
+supersonic-vortex (euler/supersonic/supersonic.cu) or three-point shock
+(euler/threepoint/threepoint.cu) problem file, compiled in (`problem`);
+`run_advection` lets the advection solver's time_integrate_rk4
+(src/2d/time_integrator.cu:89-315) take a number of steps of a fixed dt
+(a = (1,1), central flux).  Both return the state, the steps taken and the
+time.
 """
 from __future__ import annotations
 
@@ -30,7 +31,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BIN = os.path.join(HERE, "_ref", "ref_gpu_euler")
 BIN_ADVEC = os.path.join(HERE, "_ref", "ref_gpu_advec")
 BIN_PROBLEM = {"cylinder": os.path.join(HERE, "_ref", "ref_gpu_cylinder"),
-               "supersonic": os.path.join(HERE, "_ref", "ref_gpu_supersonic")}
+               "supersonic": os.path.join(HERE, "_ref", "ref_gpu_supersonic"),
+               "threepoint": os.path.join(HERE, "_ref", "ref_gpu_threepoint")}
 
 
 def build() -> str | None:
@@ -49,7 +51,8 @@ def run(mesh, order: int, c0: np.ndarray, t_end: float, timeout: float = 900.0, 
     """Advance the Euler state c0 (layout c[4][Np][E], FP64) on `mesh` (a
     dgcuda_gb300.mesh.Mesh) to t_end with the reference's solver: periodic
     meshes with problem None, else boundary sides with the hooks of the
-    reference's "cylinder" or "supersonic" problem file; RK4, or RK2 with rk2."""
+    reference's "cylinder", "supersonic" or "threepoint" problem file; RK4, or
+    RK2 with rk2."""
     binary = BIN if problem is None else BIN_PROBLEM[problem]
     return _run(binary, mesh, order, c0, 4, 0, t_end, timeout, int(bool(rk2)))
 

@@ -83,6 +83,11 @@ static int ref_printf(const char *fmt, ...) {
 #define main ref_problem_main
 #include "conservation/euler/supersonic/supersonic.cu"
 #undef main
+#elif REF_PROBLEM == 3
+// the reference's three-point shock problem file, its own hooks
+#define main ref_problem_main
+#include "conservation/euler/threepoint/threepoint.cu"
+#undef main
 #else
 #include "conservation/euler/euler.cu"
 #endif
