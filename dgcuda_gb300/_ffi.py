@@ -26,7 +26,7 @@ HOOK_MATH_DOUBLE, HOOK_MATH_REFERENCE = 0, 1
 STAGE_TIME_EXACT, STAGE_TIME_REFERENCE = 0, 1
 BC_NONE, BC_FREESTREAM, BC_EXACT, BC_PROBLEM = 0, 1, 2, 3
 IC_GAUSSIAN, IC_POLY, IC_DENSITY_WAVE, IC_VORTEX, IC_CONSTANT = 0, 1, 2, 3, 4
-IC_CYLINDER, IC_SUPERSONIC_VORTEX, IC_THREEPOINT = 5, 6, 7
+IC_CYLINDER, IC_SUPERSONIC_VORTEX, IC_THREEPOINT, IC_LINEAR = 5, 6, 7, 8
 
 
 class DgxError(RuntimeError):

@@ -696,12 +696,13 @@ namespace dgx {
 
 int project_ic_on(dgx_solver *sv, int ic, const double *params, cudaStream_t st) {
     if (!sv) return DGX_ERR_INVALID;
-    if (ic < DGX_IC_GAUSSIAN || ic > DGX_IC_THREEPOINT) { set_error("unknown initial condition %d", ic); return DGX_ERR_INVALID; }
-    if (sv->s.equation == DGX_EULER && (ic == DGX_IC_GAUSSIAN || ic == DGX_IC_POLY)) {
+    if (ic < DGX_IC_GAUSSIAN || ic > DGX_IC_LINEAR) { set_error("unknown initial condition %d", ic); return DGX_ERR_INVALID; }
+    if (sv->s.equation == DGX_EULER && (ic == DGX_IC_GAUSSIAN || ic == DGX_IC_POLY || ic == DGX_IC_LINEAR)) {
         set_error("initial condition %d is scalar", ic);
         return DGX_ERR_INVALID;
     }
-    if (sv->s.equation == DGX_ADVECTION && ic != DGX_IC_GAUSSIAN && ic != DGX_IC_POLY && ic != DGX_IC_CONSTANT) {
+    if (sv->s.equation == DGX_ADVECTION && ic != DGX_IC_GAUSSIAN && ic != DGX_IC_POLY && ic != DGX_IC_CONSTANT &&
+        ic != DGX_IC_LINEAR) {
         set_error("initial condition %d needs the Euler equations", ic);
         return DGX_ERR_INVALID;
     }
@@ -832,7 +833,7 @@ int dgx_solver_set_boundary(dgx_solver *sv, int kind, int ic, const double *para
         return DGX_OK;
     }
     case DGX_BC_EXACT:
-        if (s.equation != DGX_ADVECTION || ic < DGX_IC_GAUSSIAN || ic > DGX_IC_POLY) {
+        if (s.equation != DGX_ADVECTION || (ic != DGX_IC_GAUSSIAN && ic != DGX_IC_POLY && ic != DGX_IC_LINEAR)) {
             set_error("the exact Dirichlet boundary needs advection and a scalar initial condition");
             return DGX_ERR_INVALID;
         }

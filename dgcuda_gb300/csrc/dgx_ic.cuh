@@ -40,6 +40,7 @@ __device__ inline void ic_eval(int ic, const double *P, double g, double x, doub
         break;
     }
     case DGX_IC_POLY: U[0] = pow(x - y, P[0]); break;
+    case DGX_IC_LINEAR: U[0] = P[0] + P[1] * x + P[2] * y; break;
     case DGX_IC_DENSITY_WAVE: {
         const double rho = 1.0 + P[0] * sin(2.0 * pi * P[4] * (x + y));
         U[0] = rho; U[1] = rho * P[1]; U[2] = rho * P[2];

@@ -86,6 +86,11 @@ enum dgx_dt_mode { DGX_DT_FIXED = 0, DGX_DT_CFL = 1 };
  *   THREEPOINT    oblique shock state for atan(x/y) < theta, gas at rest
  *                 beyond                                 {M, theta in degrees}
  *                 (euler/threepoint/threepoint.cu:27-54; PI = 3.14159 as there)
+ *   LINEAR        u = c0 + cx x + cy y (advection)       {c0, cx, cy}
+ *                 (the reference's advection problem is u0 = x + y,
+ *                 2dadvec/2dadvec_kernels.cu:176-178, with the exact
+ *                 Dirichlet data x - 2t + y at its boundary sides, :184-186:
+ *                 DGX_BC_EXACT with {0, 1, 1} and a = (1, 1))
  * Lx, Ly > 0 take distances to the nearest periodic image. */
 enum dgx_ic {
     DGX_IC_GAUSSIAN = 0,
@@ -95,7 +100,8 @@ enum dgx_ic {
     DGX_IC_CONSTANT = 4,
     DGX_IC_CYLINDER = 5,
     DGX_IC_SUPERSONIC_VORTEX = 6,
-    DGX_IC_THREEPOINT = 7
+    DGX_IC_THREEPOINT = 7,
+    DGX_IC_LINEAR = 8
 };
 
 typedef struct dgx_mesh dgx_mesh;
@@ -275,8 +281,9 @@ int dgx_write_vertex_values(dgx_solver *solver, const char *path_pattern);
  *     src/2d/conservation/euler/cylinder/cylinder.cu:58-111, with the side normal);
  *   Euler, -2 outflow / -3 inflow: DGX_BC_FREESTREAM params {rho, u, v, p}
  *     (the problem hooks U_outflow / U_inflow, euler.cu:177-241);
- *   advection, any tag: DGX_BC_EXACT, the initial condition `ic` with `params`
- *     translated by a*t (the reference's boundary_exact, 2dadvec_kernels.cu:184-186);
+ *   advection, any tag: DGX_BC_EXACT, the initial condition `ic` (GAUSSIAN, POLY
+ *     or LINEAR) with `params` translated by a*t (the reference's boundary_exact,
+ *     2dadvec_kernels.cu:184-186, is LINEAR {0, 1, 1} at a = (1, 1));
  *   Euler, DGX_BC_PROBLEM with ic = CYLINDER / SUPERSONIC_VORTEX / THREEPOINT and
  *     that initial condition's params: the problem file's own hooks for all
  *     three tags --

@@ -310,6 +310,8 @@ enum {
     ORC_IC_CYLINDER = 5,      /* free stream rho = gamma, u = M, p = 1         params M */
     ORC_IC_SUPERSONIC = 6,    /* supersonic vortex between two arcs            params M A */
     ORC_IC_THREEPOINT = 7,    /* oblique shock state inside the angle theta    params M theta_deg */
+    ORC_IC_LINEAR = 8,        /* u = c0 + cx x + cy y (advection u0 = x + y,   params c0 cx cy
+                                 2dadvec/2dadvec_kernels.cu:176-178) */
 };
 
 /* the reference's problem files define PI as 3.14159 (threepoint.cu:13) */
@@ -890,6 +892,7 @@ void orc_ic_eval(int ic, const double *P, double g, double x, double y, double *
         break;
     }
     case ORC_IC_POLY: U[0] = pow(x - y, P[0]); break;
+    case ORC_IC_LINEAR: U[0] = P[0] + P[1] * x + P[2] * y; break;
     case ORC_IC_DENSITY_WAVE: {
         double rho = 1.0 + P[0] * sin(2.0 * pi * P[4] * (x + y));
         U[0] = rho; U[1] = rho * P[1]; U[2] = rho * P[2];

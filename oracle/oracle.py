@@ -19,7 +19,7 @@ REF_BIN = os.path.join(HERE, "_ref", "ref_euler")
 ADVECTION, EULER = 0, 1
 CENTRAL, LLF = 0, 1
 IC_GAUSSIAN, IC_POLY, IC_DENSITY_WAVE, IC_VORTEX, IC_CONSTANT = 0, 1, 2, 3, 4
-IC_CYLINDER, IC_SUPERSONIC, IC_THREEPOINT = 5, 6, 7
+IC_CYLINDER, IC_SUPERSONIC, IC_THREEPOINT, IC_LINEAR = 5, 6, 7, 8
 RK4, RK2, FE = 0, 1, 2
 
 _lib = None

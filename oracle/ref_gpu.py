@@ -59,7 +59,9 @@ def run(mesh, order: int, c0: np.ndarray, t_end: float, timeout: float = 900.0, 
 
 def run_advection(mesh, order: int, c0: np.ndarray, dt: float, steps: int, timeout: float = 900.0) -> dict:
     """`steps` RK4 steps of dt of the advection state c0 (c[Np][E], FP64) on
-    `mesh` (periodic) with the reference's advection solver (a = (1,1))."""
+    `mesh` with the reference's advection solver (a = (1,1)): periodic, or
+    with boundary sides tagged -1, whose ghost value is the reference's exact
+    data x - 2t + y (2dadvec_kernels.cu:184-186) at t = the step's start."""
     return _run(BIN_ADVEC, mesh, order, c0, 1, int(steps), dt, timeout, 0)
 
 

@@ -18,7 +18,11 @@
 //    and wrappers) and src/2d/{time_integrator,quadrature,basis}.cu.  The
 //    driver repeats src/2d/main.cu:40-196 the same way and calls that
 //    time_integrate_rk4 (src/2d/time_integrator.cu:89-315) unchanged (fixed dt,
-//    a number of steps).
+//    a number of steps); boundary sides tagged -1 take its exact data
+//    (boundary_exact, 2dadvec_kernels.cu:184-186).
+//  * Euler with a problem file's own hooks (-DREF_PROBLEM=1, 2, 3: the
+//    cylinder, supersonic-vortex and three-point files) for meshes with
+//    boundary sides.
 //
 // Three build adaptations, made here rather than in the reference's files:
 //  * cudaThreadSynchronize (removed in CUDA 13) maps to cudaDeviceSynchronize;
@@ -32,7 +36,7 @@
 // printf is routed to a counter: the Euler time loop prints "\rt = ..." once
 // per step, which gives the number of steps taken.
 //
-// Usage: ref_gpu_euler|ref_gpu_cylinder|ref_gpu_supersonic|ref_gpu_advec <in.bin> <out.bin>
+// Usage: ref_gpu_euler|ref_gpu_cylinder|ref_gpu_supersonic|ref_gpu_threepoint|ref_gpu_advec <in.bin> <out.bin>
 //   in:  int32 E, S, p, steps, rk2 (Euler: 1 runs time_integrate_rk2), 0;
 //        double t (Euler: end time; advection: dt);
 //        double V[6][E] (V1x V1y V2x V2y V3x V3y); int32 elem_s[3][E];
@@ -183,10 +187,14 @@ int main(int argc, char **argv) {
     std::fclose(fi);
     for (size_t s = 0; s < S; ++s) {
         const int L = sd[s], R = sd[S + s], ls = sd[2 * S + s], rs = sd[3 * S + s];
-        // boundary sides (-1 reflecting, -2 outflow, -3 inflow) only with a problem file's hooks
-        const bool bnd_ok = !REF_ADVECTION && REF_PROBLEM != 0 && R >= -3 && R <= -1;
+        // boundary sides: Euler -1 reflecting, -2 outflow, -3 inflow only with a
+        // problem file's hooks; advection -1, the exact data of its
+        // boundary_exact (2dadvec_kernels.cu:184-186), with a right side number
+        // in 0..2 (its surface kernel indexes the side tables by it)
+        const bool bnd_ok = REF_ADVECTION ? (R == -1 && rs >= 0 && rs <= 2)
+                                          : (REF_PROBLEM != 0 && R >= -3 && R <= -1);
         if (L < 0 || L >= num_elem || ls < 0 || ls > 2 || ((R < 0 || R >= num_elem || rs < 0 || rs > 2) && !bnd_ok)) {
-            std::fprintf(stderr, "side %zu: the harness takes periodic meshes only, or boundary sides with a problem file\n", s);
+            std::fprintf(stderr, "side %zu: the harness takes periodic meshes, advection boundary sides -1, or Euler boundary sides with a problem file\n", s);
             return 2;
         }
     }

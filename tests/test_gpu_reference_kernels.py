@@ -6,8 +6,12 @@ advection time_integrate_rk4, src/2d/time_integrator.cu:89-315, unchanged).
 Advection: the reference hard-wires a = (1,1) and the central flux
 (src/2d/2dadvec/2dadvec_kernels.cu:150-164); both sides take the same number of
 steps of the same fixed dt from the same FP64 coefficients.  Its side lengths
-and normals also use float square roots.  Tolerances: FP64 path <= 1e-9, FP32
-path <= 1e-5.
+and normals also use float square roots.  On meshes with boundary sides (-1)
+the reference takes the exact data of its problem, x - 2t + y
+(boundary_exact, 2dadvec_kernels.cu:184-186) at t = the step's start
+(src/2d/time_integrator.cu:144-145) in every stage; the GPU path takes
+DGX_BC_EXACT with DGX_IC_LINEAR {0, 1, 1} and the reference's stage times.
+Tolerances: FP64 path <= 1e-9, FP32 path <= 1e-5.
 
 Euler:
 
@@ -27,7 +31,7 @@ import numpy as np
 import pytest
 
 from dgcuda_gb300 import _ffi
-from dgcuda_gb300.mesh import periodic_square
+from dgcuda_gb300.mesh import from_triangles, periodic_square
 from dgcuda_gb300.solver import Solver
 
 torch = pytest.importorskip("torch")
@@ -118,5 +122,70 @@ def test_advection_matches_reference_gpu_solver(ref_gpu, p):
         errs[name] = np.linalg.norm(s_ - ref["state"]) / np.linalg.norm(ref["state"])
     print(f"advection p={p}: {steps} steps, FP64 vs reference {errs['fp64']:.2e}, "
           f"FP32 vs reference {errs['fp32']:.2e}")
+    assert errs["fp64"] <= 1e-9, errs
+    assert errs["fp32"] <= 1e-5, errs
+
+
+def walled_square(n, seed):
+    """[0,1]^2 in n x n cells, interior vertices jittered by 0.15 h, two
+    counter-clockwise triangles per cell, numbered by the reference's
+    converter's rules (from_triangles); every boundary side -1 with right
+    side number 0, as in the reference's mesh files."""
+    rng = np.random.default_rng(seed)
+    g = np.linspace(0.0, 1.0, n + 1)
+    X, Y = np.meshgrid(g, g, indexing="xy")
+    inner = (X > 0) & (X < 1) & (Y > 0) & (Y < 1)
+    X = X + inner * rng.uniform(-0.15, 0.15, X.shape) / n
+    Y = Y + inner * rng.uniform(-0.15, 0.15, Y.shape) / n
+    xy = np.stack([X.ravel(), Y.ravel()], axis=1)
+    v = lambda i, j: j * (n + 1) + i
+    tris = []
+    for j in range(n):
+        for i in range(n):
+            tris.append((v(i, j), v(i + 1, j), v(i + 1, j + 1)))
+            tris.append((v(i, j), v(i + 1, j + 1), v(i, j + 1)))
+    return from_triangles(xy, tris, lambda a, b: -1)
+
+
+@pytest.mark.parametrize("p", [0, 1, 2, 3])
+def test_advection_boundary_matches_reference_gpu_solver(ref_gpu, p):
+    """A pulse on the reference's linear state x + y in a walled square: its
+    boundary sides take the reference's exact data x - 2t + y."""
+    n = 12
+    mesh = walled_square(n, seed=50 + p)
+    assert (mesh.right_elem < 0).sum() == 4 * n
+    init = Solver(mesh, p, _ffi.ADVECTION, _ffi.FLUX_CENTRAL, _ffi.FP64)
+    init.project(_ffi.IC_GAUSSIAN, (0.4, 0.6, 0.02, 0.0, 0.0))
+    pulse = init.get_state()
+    init.project(_ffi.IC_LINEAR, (0.0, 1.0, 1.0))
+    c0 = pulse + init.get_state()
+    init.close()
+    dt = 0.1 * (1.0 / n) / (np.sqrt(2.0) * (2 * p + 1))
+    steps = 25
+    ref = ref_gpu.run_advection(mesh, p, c0, dt, steps)
+    assert ref["steps"] == steps
+    assert np.all(np.isfinite(ref["state"]))
+    errs = {}
+    for name, prec in (("fp64", _ffi.FP64), ("fp32", _ffi.FP32)):
+        sv = Solver(mesh, p, _ffi.ADVECTION, _ffi.FLUX_CENTRAL, prec)
+        sv.set_boundary(_ffi.BC_EXACT, _ffi.IC_LINEAR, (0.0, 1.0, 1.0))
+        sv.set_option(_ffi.OPT_STAGE_TIME, _ffi.STAGE_TIME_REFERENCE)
+        sv.set_state(c0)
+        sv.set_dt(dt)
+        k, _ = sv.run(max_steps=steps)
+        assert k == steps
+        s_ = sv.get_state().reshape(-1)
+        sv.close()
+        errs[name] = np.linalg.norm(s_ - ref["state"]) / np.linalg.norm(ref["state"])
+    # the boundary data matter: with the interior trace as ghost the state differs
+    sv = Solver(mesh, p, _ffi.ADVECTION, _ffi.FLUX_CENTRAL, _ffi.FP64)
+    sv.set_state(c0)
+    sv.set_dt(dt)
+    sv.run(max_steps=steps)
+    off = np.linalg.norm(sv.get_state().reshape(-1) - ref["state"]) / np.linalg.norm(ref["state"])
+    sv.close()
+    print(f"advection with boundary p={p}: {steps} steps, FP64 vs reference {errs['fp64']:.2e}, "
+          f"FP32 vs reference {errs['fp32']:.2e} (interior-trace ghost: {off:.2e})")
+    assert off > 1e3 * max(errs["fp64"], 1e-12)
     assert errs["fp64"] <= 1e-9, errs
     assert errs["fp32"] <= 1e-5, errs

@@ -125,3 +125,24 @@ def test_advection_convergence(oracle_mod):
         errs.append(np.linalg.norm(c1 - exact) / np.linalg.norm(exact))
     rate = math.log2(errs[0] / errs[1])
     assert rate > 2.3, errs
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+@pytest.mark.parametrize("flux", ["central", "llf"])
+def test_advection_linear_exact_boundary(p, flux, oracle_mod):
+    """The reference's advection problem (2dadvec_kernels.cu:176-186): u0 = x + y
+    with exact Dirichlet data x - 2t + y at every boundary side, a = (1, 1).
+    For p >= 1 the exact solution lies in the space and RK4 integrates its
+    linear time dependence exactly, so the scheme keeps it to rounding: after
+    the steps the state is the projection of x + y - 2t."""
+    from dgcuda_gb300.mesh import dirichlet_square
+    orc = oracle_mod
+    m = dirichlet_square(8, jitter=0.1, seed=3, tag=-1)
+    o = orc.Oracle(m, p, orc.ADVECTION, orc.CENTRAL if flux == "central" else orc.LLF, a=(1.0, 1.0))
+    o.set_boundary(2, orc.IC_LINEAR, (0.0, 1.0, 1.0))
+    c0 = o.project(orc.IC_LINEAR, (0.0, 1.0, 1.0))
+    dt = 0.1 / 8 / (2 * p + 1)
+    c, n, t = o.run(c0, t_end=1.0, dt=dt, max_steps=12)
+    assert n == 12
+    exact = o.project(orc.IC_LINEAR, (-2.0 * t, 1.0, 1.0))
+    assert np.abs(c - exact).max() <= 1e-12 * np.abs(exact).max()
