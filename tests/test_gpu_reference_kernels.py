@@ -57,8 +57,8 @@ def rel_l2(a, b):
     return np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
 
 
-def ours(mesh, p, precision, c0, t_end):
-    sv = Solver(mesh, p, _ffi.EULER, _ffi.FLUX_LLF, precision)
+def ours(mesh, p, precision, c0, t_end, integrator=_ffi.RK4):
+    sv = Solver(mesh, p, _ffi.EULER, _ffi.FLUX_LLF, precision, integrator=integrator)
     sv.set_state(c0)
     sv.set_dt(None, cfl=0.7)
     n, t = sv.run(t_end=t_end)
@@ -91,6 +91,34 @@ def test_paths_match_reference_gpu_solver(ref_gpu, case):
     err64 = rel_l2(s64, ref["state"]).max()
     err32 = rel_l2(s32, ref["state"]).max()
     print(f"{case[0]}: {ref['steps']} steps, FP64 vs reference {err64:.2e}, FP32 vs reference {err32:.2e}")
+    assert err64 <= 1e-9, err64
+    assert err32 <= 1e-5, err32
+
+
+@pytest.mark.parametrize("case", [
+    ("vortex", 16, 10.0, 2, _ffi.IC_VORTEX, VORTEX, 0.25),
+    ("density wave", 12, 1.0, 3, _ffi.IC_DENSITY_WAVE, WAVE, 0.02),
+], ids=lambda c: c[0])
+def test_rk2_matches_reference_gpu_solver(ref_gpu, case):
+    """RK2 midpoint on periodic meshes against the reference's own
+    time_integrate_rk2 (src/2d/conservation/time_integrator.cu:466-614): the
+    same CFL rule, steps and end time."""
+    _, n, L, p, ic, params, t_end = case
+    mesh = periodic_square(n, lx=L, ly=L, jitter=0.15, seed=21 + n)
+    init = Solver(mesh, p, _ffi.EULER, _ffi.FLUX_LLF, _ffi.FP64)
+    init.project(ic, params)
+    c0 = init.get_state()
+    init.close()
+    ref = ref_gpu.run(mesh, p, c0, t_end, rk2=True)
+    assert ref["steps"] > 2
+    assert rel_l2(ref["state"], c0).max() > 1e-4, "the reference solver did not move the state"
+    s64, n64, t64 = ours(mesh, p, _ffi.FP64, c0, t_end, _ffi.RK2)
+    s32, n32, _ = ours(mesh, p, _ffi.FP32, c0, t_end, _ffi.RK2)
+    assert n64 == ref["steps"] and n32 == ref["steps"]
+    assert t64 == pytest.approx(t_end, rel=1e-12)
+    err64 = rel_l2(s64, ref["state"]).max()
+    err32 = rel_l2(s32, ref["state"]).max()
+    print(f"rk2 {case[0]}: {ref['steps']} steps, FP64 vs reference {err64:.2e}, FP32 vs reference {err32:.2e}")
     assert err64 <= 1e-9, err64
     assert err32 <= 1e-5, err32
 
