@@ -2,8 +2,8 @@
  * dgx_oracle.c -- FP64 CPU oracle of the reference 2D modal DG scheme.
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links or calls this
- * file; it is used by tests/, by __graft_entry__.smoke() and by the CPU-baseline
- * leg of bench.py, as the checker of the CUDA path.
+ * file; tests/ and __graft_entry__.smoke() test the CUDA path against it, and
+ * the CPU-baseline leg of bench.py times it.
  *
  * It restates, in plain C with OpenMP over edges and elements, the reference
  * (thePerv/DGCUDA) algorithm for one RHS evaluation and the classic RK4 step:

@@ -1,8 +1,8 @@
 """ctypes wrapper of the FP64 CPU oracle (oracle/dgx_oracle.c).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()`` and
-by the CPU-baseline leg of ``bench.py`` as the checker of the CUDA path; the
-product package never imports it.
+TEST INFRASTRUCTURE ONLY: imported by tests/ and ``__graft_entry__.smoke()``
+(the oracle the CUDA path is tested against) and by the CPU-baseline leg of
+``bench.py`` (timed as the CPU baseline); the product package never imports it.
 """
 from __future__ import annotations
 

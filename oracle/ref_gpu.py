@@ -1,4 +1,4 @@
-"""TEST INFRASTRUCTURE ONLY: the reference's own CUDA solvers as checkers and a
+"""TEST INFRASTRUCTURE ONLY: the reference's own CUDA solvers as test references and a
 reported baseline, never as the product path.
 
 `oracle/_ref/ref_gpu_euler` and `ref_gpu_advec` are built by `make -C oracle

@@ -1,4 +1,4 @@
-// ref_gpu_harness.cu -- TEST INFRASTRUCTURE ONLY (a checker and a reported
+// ref_gpu_harness.cu -- TEST INFRASTRUCTURE ONLY (a test reference and a reported
 // baseline, never the product path).
 //
 // Runs the reference's own CUDA solvers, compiled from its unmodified sources,
