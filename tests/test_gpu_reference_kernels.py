@@ -86,13 +86,17 @@ def test_paths_match_reference_gpu_solver(ref_gpu, case):
     assert rel_l2(ref["state"], c0).max() > 1e-4, "the reference solver did not move the state"
     s64, n64, t64 = ours(mesh, p, _ffi.FP64, c0, t_end)
     s32, n32, _ = ours(mesh, p, _ffi.FP32, c0, t_end)
-    assert n64 == ref["steps"] and n32 == ref["steps"]
+    s32c, n32c, _ = ours(mesh, p, _ffi.FP32_COMP, c0, t_end)
+    assert n64 == ref["steps"] and n32 == ref["steps"] and n32c == ref["steps"]
     assert t64 == pytest.approx(t_end, rel=1e-12)
     err64 = rel_l2(s64, ref["state"]).max()
     err32 = rel_l2(s32, ref["state"]).max()
-    print(f"{case[0]}: {ref['steps']} steps, FP64 vs reference {err64:.2e}, FP32 vs reference {err32:.2e}")
+    err32c = rel_l2(s32c, ref["state"]).max()
+    print(f"{case[0]}: {ref['steps']} steps, FP64 vs reference {err64:.2e}, FP32 vs reference {err32:.2e}, "
+          f"compensated FP32 vs reference {err32c:.2e}")
     assert err64 <= 1e-9, err64
     assert err32 <= 1e-5, err32
+    assert err32c <= 1e-5, err32c
 
 
 @pytest.mark.parametrize("case", [
