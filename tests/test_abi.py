@@ -80,3 +80,30 @@ def test_mesh_validation_on_host(defect, native):
     rc, msg = _create(m)
     assert rc == _ffi.ERR_INVALID, msg
     assert msg
+
+
+def header_constants():
+    """Every enumerator `DGX_NAME = value` the headers declare."""
+    out = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for body in re.findall(r"enum\s+\w*\s*\{(.*?)\}", text, flags=re.S):
+            for name, val in re.findall(r"\b(DGX_[A-Z0-9_]+)\s*=\s*(-?\d+)", body):
+                out[name] = int(val)
+    return out
+
+
+def test_binding_constants_match_header():
+    """The ctypes binding's constants are the header's enumerators (every one
+    the binding names), so Python callers and C callers pass the same codes."""
+    hdr = header_constants()
+    assert hdr["DGX_IC_LINEAR"] == 8 and hdr["DGX_FP32_COMP"] == 3
+    matched = 0
+    for name, val in hdr.items():
+        short = name[4:]
+        if hasattr(_ffi, short):
+            assert getattr(_ffi, short) == val, name
+            matched += 1
+    for short in ("IC_LINEAR", "IC_THREEPOINT", "BC_EXACT", "FP32_COMP", "RK2", "FLUX_LLF", "OPT_HOOK_MATH"):
+        assert "DGX_" + short in hdr and hasattr(_ffi, short), short
+    assert matched >= 40, matched
